@@ -1,0 +1,386 @@
+#!/usr/bin/env python
+"""Benchmark of the clustered-forward light-culling path on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload plain_large|plain_small]
+
+A step is one culling pass over one view: light transform, sphere-AABB
+culling and the offset scan (the per-frame work of PipelineLightCulling; the
+AABBs are generated once per projection, as the reference's dirty flag does).
+The default workload is the 2560x1600, 32x18x48-cluster view with 16384
+lights in Gaussian blobs.  The metric is light-cluster tests per second
+counted brute force (clusters x lights per view); views/s is the same rate
+per view.
+
+ours       value: device-resident inputs, each step timed with CUDA events on
+           the launching stream, L2 flushed (256 MiB write) between steps.
+           e2e:   the same step through the C ABI with host buffers: pinned
+           LightData upload, the pipeline call, and the LightCell + index
+           read-back, timed on the host clock with synchronisation.
+           roofline: the culling kernel's own event-timed duration against the
+           FP32 issue rate (16 ops per executed test).
+           cpu_baseline: the reference's LightCulling.comp compiled as C++
+           (or the oracle port where that is unavailable) on all host cores.
+reference  the same CPU implementation alone, timed per step on a bounded
+           sample (a run of depth slices) of the same view.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import platform
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+import numpy as np  # noqa: E402
+
+METRIC = "light-cluster tests/s"
+UNIT = "tests/s"
+OPS_PER_TEST = 16
+L2_FLUSH_BYTES = 256 << 20
+SMS = 152
+FP32_LANES_PER_SM = 128
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=1000)
+    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--workload", choices=["plain_large", "plain_small"], default="plain_large")
+    p.add_argument("--tuning", type=str, default="", help="K,warps,tile,stages of the culling kernel")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline budget")
+    return p.parse_args()
+
+
+def make_view(name: str, rank: int):
+    from hellovulkan_gb300 import scenes
+    if name == "plain_small":
+        return scenes.plain_small(1 + 1000 * rank)
+    return scenes.plain_large(2 + 1000 * rank)
+
+
+def workload_config(view, name):
+    x, y, z = view.grid
+    w, h = view.ubo.screenSize
+    return {"workload": "%s: %dx%d, grid %dx%dx%d = %d clusters, %d lights, cap %d" % (
+        name, w, h, x, y, z, view.clusters, view.light_count, view.cap),
+        "clusters": view.clusters, "lights": view.light_count, "cap": view.cap,
+        "tests_per_view": view.clusters * view.light_count}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait(timeout=5)
+        self.file.flush()
+        rows = [l.split(",") for l in Path(self.file.name).read_text().splitlines() if l.strip()]
+        os.unlink(self.file.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [c.strip() for c in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- CPU side
+def cpu_impl():
+    """(kind, object with .cull(ubo, aabbs, lights, threads)) — the reference's
+    shaders compiled as C++ when available, else the oracle port."""
+    from oracle import Oracle, Reference
+    ref = Reference.load()
+    if ref is not None:
+        return "reference", lambda ubo, a, L, cap, t: ref.cull(ubo, a, L, threads=t)
+    o = Oracle()
+    return "port", lambda ubo, a, L, cap, t: o.cull(ubo, a, L, cap, threads=t)[:2]
+
+
+def sub_view(ubo, aabbs, k0: int, nz: int):
+    """The clusters of depth slices [k0, k0+nz) as a view of their own."""
+    import copy
+    u = copy.copy(ubo)
+    u.sliceCountZ = nz
+    per = int(ubo.sliceCountX) * int(ubo.sliceCountY)
+    return u, aabbs[k0 * per:(k0 + nz) * per]
+
+
+def cpu_threads() -> int:
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+
+
+def time_cpu(view, aabbs, budget_s: float, steps: int | None = None, warmup: int = 1):
+    """Times the CPU implementation on slice samples; returns a dict."""
+    kind, cull = cpu_impl()
+    threads = cpu_threads()
+    X, Y, Z = view.grid
+    # size the per-step sample: as many depth slices as fit the budget
+    u1, a1 = sub_view(view.ubo, aabbs, 0, 1)
+    t0 = time.perf_counter()
+    cull(u1, a1, view.lights, view.cap, threads)
+    one = max(time.perf_counter() - t0, 1e-4)
+    n_steps = steps if steps is not None else 5
+    per_step = budget_s / max(n_steps, 1)
+    nz = int(max(1, min(Z, per_step / one)))
+    times, tests = [], 0
+    for i in range(warmup + n_steps):
+        k0 = (i * nz) % max(1, Z - nz + 1)
+        u, a = sub_view(view.ubo, aabbs, k0, nz)
+        t0 = time.perf_counter()
+        cull(u, a, view.lights, view.cap, threads)
+        dt = time.perf_counter() - t0
+        if i >= warmup:
+            times.append(dt)
+            tests += X * Y * nz * view.light_count
+    total = sum(times)
+    return {"kind": kind, "cores": threads, "value": tests / total, "ms_per_step": 1e3 * total / len(times),
+            "sample": "%d of %d depth slices (%d clusters x %d lights) per step, %d steps, %s threads" % (
+                nz, Z, X * Y * nz, view.light_count, len(times), threads),
+            "cpu": platform.processor() or platform.machine()}
+
+
+def run_reference_arm(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import Oracle
+    view = make_view(args.workload, 0)
+    aabbs = Oracle().generate_aabbs(view.ubo)
+    budget = min(150.0, max(10.0, 0.05 * (args.steps + args.warmup)))
+    r = time_cpu(view, aabbs, budget, steps=args.steps, warmup=args.warmup)
+    cfg = workload_config(view, args.workload)
+    line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "impl": "reference",
+            "config": cfg,
+            "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": r["kind"],
+                             "sample": r["sample"]},
+            "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------- GPU side
+def run_ours(args):
+    import torch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from hellovulkan_gb300 import build as cuda_build
+    cuda_build.build()
+    from hellovulkan_gb300.pipelines import (Context, PipelineAABBGenerator, PipelineLightCulling,
+                                             ResourcesClusterForward, ResourcesLight)
+
+    view = make_view(args.workload, rank)
+    ctx = Context(local)
+    rl = ResourcesLight(ctx)
+    rl.add_lights(view.lights)
+    rc = ResourcesClusterForward(ctx)
+    rc.create_buffers(*view.grid, view.cap)
+    gen = PipelineAABBGenerator(ctx, rc)
+    cull = PipelineLightCulling(ctx, rl, rc)
+    if args.tuning:
+        cull.set_tuning(*[int(t) for t in args.tuning.split(",")])
+    stream = torch.cuda.Stream()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    # AABBs: once per projection (timed for information)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    gen.set_cluster_forward_ubo(view.ubo)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        gen.fill_command_buffer(stream)
+        e1.record(stream)
+    stream.synchronize()
+    aabb_ms = e0.elapsed_time(e1)
+
+    cull.set_cluster_forward_ubo(view.ubo)
+    cull.enable_stage_timing(True)
+    for _ in range(args.warmup):
+        cull.fill_command_buffer(stream)
+    stream.synchronize()
+
+    sampler = ClockSampler(local).start()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stage = np.zeros((args.steps, 3))
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        starts[i].record(stream)
+        cull.fill_command_buffer(stream)
+        ends[i].record(stream)
+        stage[i] = cull.stage_times_ms()
+    torch.cuda.synchronize()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = float(sum(step_ms))
+
+    # e2e through the C ABI with host buffers
+    b = rc.buffers()
+    h_lights = torch.from_numpy(np.ascontiguousarray(view.lights)).pin_memory()
+    h_cells = torch.empty((b.cluster_count, 2), dtype=torch.int32).pin_memory()
+    h_idx = torch.empty(b.index_capacity, dtype=torch.int32).pin_memory()
+    cells_np, idx_np = h_cells.numpy().view(np.uint32), h_idx.numpy().view(np.uint32)
+    e2e_steps = max(1, min(args.steps, 500))
+    cull.enable_stage_timing(False)
+    for _ in range(3):
+        rl.upload_async(h_lights, view.light_count, stream)
+        cull.set_cluster_forward_ubo(view.ubo)
+        cull.fill_command_buffer(stream)
+        _, got = rc.read_outputs(stream, cells_np, idx_np)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    total_indices = 0
+    for _ in range(e2e_steps):
+        rl.upload_async(h_lights, view.light_count, stream)
+        cull.set_cluster_forward_ubo(view.ubo)
+        cull.fill_command_buffer(stream)
+        _, got = rc.read_outputs(stream, cells_np, idx_np)
+        total_indices = got.size
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    clocks = sampler.stop()
+
+    # correctness of what was timed (rank 0, last result) against the oracle
+    tests_per_view = view.clusters * view.light_count
+    stats = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device="cuda")
+    if ws > 1:
+        torch.distributed.all_reduce(stats, op=torch.distributed.ReduceOp.MAX)
+    total_ms, e2e_s = float(stats[0]), float(stats[1])
+    if rank != 0:
+        torch.distributed.destroy_process_group()
+        return
+
+    from oracle import Oracle
+    o = Oracle()
+    o_aabbs = o.generate_aabbs(view.ubo)
+    o_cells, o_idx, executed = o.cull(view.ubo, o_aabbs, view.lights, view.cap)
+    parity = bool(np.array_equal(cells_np, o_cells) and np.array_equal(idx_np[: o_idx.size], o_idx)
+                  and total_indices == o_idx.size)
+
+    value = ws * tests_per_view * args.steps / (total_ms * 1e-3)
+    cull_ms = float(np.mean(stage[:, 1]))
+    achieved = executed * OPS_PER_TEST / (cull_ms * 1e-3) / 1e12
+    sm_max = clocks.get("sm_max_mhz") or 2070.0
+    peak = SMS * FP32_LANES_PER_SM * sm_max * 1e6 / 1e12
+    traffic = None
+    prof = REPO / "profiles" / "cull_dram_bytes.json"
+    if prof.exists():
+        try:
+            traffic = json.loads(prof.read_text()).get(args.workload)
+        except ValueError:
+            traffic = None
+    alg_bytes = 16 * view.light_count + 32 * view.clusters + 4 * view.clusters + 4 * o_idx.size
+    peaks = {}
+    try:
+        peaks = json.loads((REPO / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    bi = view.light_count * 48
+    bo = view.clusters * 8 + total_indices * 4 + 4
+    cpu = None
+    if not args.no_cpu_baseline:
+        r = time_cpu(view, o_aabbs, args.cpu_seconds)
+        cpu = {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": r["kind"], "sample": r["sample"],
+               "cpu": r["cpu"]}
+    cfg = workload_config(view, args.workload)
+    cfg.update({"parallelism": "replicas x%d" % ws if ws > 1 else "single GPU",
+                "l2": "flushed between timed steps (256 MiB write)",
+                "aabbs": "generated once per projection (%.4f ms, not in the step)" % aabb_ms,
+                "step": "light transform + culling + offset scan"})
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded)", "config": cfg,
+        "views_per_s": ws * args.steps / (total_ms * 1e-3),
+        "parity_with_oracle": parity,
+        "stage_ms": {"light_transform": float(np.mean(stage[:, 0])), "cull": cull_ms,
+                     "offset_scan": float(np.mean(stage[:, 2]))},
+        "executed_tests_per_view": executed,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "Tops/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "cull_kernel", "ops_per_launch": executed * OPS_PER_TEST,
+                     "peak_source": "nominal FP32 issue rate, %d SMs x %d lanes x %.0f MHz (no measured FP32 peak "
+                                    "exists in MEASURED_PEAKS.json)" % (SMS, FP32_LANES_PER_SM, sm_max)},
+        "roofline_hbm": {"achieved": alg_bytes / (cull_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": alg_bytes / (cull_ms * 1e-3) / 1e9 / hbm_peak, "bytes_per_launch": alg_bytes},
+        "cpu_baseline": cpu,
+        "e2e": {"value": ws * tests_per_view * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": bi,
+                "d2h_bytes_per_step": bo, "ms_per_step": 1e3 * e2e_s / e2e_steps, "steps": e2e_steps,
+                "timing": "host clock, synchronised, pinned host buffers"},
+        "gpu_launches": 3 * (args.steps + e2e_steps),
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,176 @@
+"""ctypes binding of libcfcull.so (include/cfcull.h).
+
+The library is the product: when it is missing this module raises instead of
+falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+REPO = PKG.parent
+LIB_PATH = PKG / "libcfcull.so"
+HEADERS = [REPO / "include" / "cfcull.h"]
+
+
+class CfLightData(C.Structure):
+    _fields_ = [("position", C.c_float * 4), ("color", C.c_float * 4), ("radius", C.c_float), ("_pad", C.c_float * 3)]
+
+
+class CfAABB(C.Structure):
+    _fields_ = [("minPoint", C.c_float * 4), ("maxPoint", C.c_float * 4)]
+
+
+class CfLightCell(C.Structure):
+    _fields_ = [("offset", C.c_uint32), ("count", C.c_uint32)]
+
+
+class CfClusterForwardUBO(C.Structure):
+    _fields_ = [
+        ("cameraInverseProjection", C.c_float * 16),
+        ("cameraView", C.c_float * 16),
+        ("screenSize", C.c_float * 2),
+        ("sliceScaling", C.c_float),
+        ("sliceBias", C.c_float),
+        ("cameraNear", C.c_float),
+        ("cameraFar", C.c_float),
+        ("sliceCountX", C.c_uint32),
+        ("sliceCountY", C.c_uint32),
+        ("sliceCountZ", C.c_uint32),
+        ("_pad", C.c_uint32 * 3),
+    ]
+
+
+class CfClusterForwardBuffers(C.Structure):
+    _fields_ = [
+        ("aabbs", C.c_void_p),
+        ("light_cells", C.c_void_p),
+        ("light_indices", C.c_void_p),
+        ("total_indices", C.c_void_p),
+        ("cluster_count", C.c_uint32),
+        ("max_lights_per_cluster", C.c_uint32),
+        ("index_capacity", C.c_uint64),
+    ]
+
+
+assert C.sizeof(CfLightData) == 48 and C.sizeof(CfAABB) == 32 and C.sizeof(CfLightCell) == 8
+assert C.sizeof(CfClusterForwardUBO) == 176
+
+STATUS = {
+    0: "CF_SUCCESS", 1: "CF_ERROR_INVALID_ARGUMENT", 2: "CF_ERROR_OUT_OF_MEMORY", 3: "CF_ERROR_CUDA",
+    4: "CF_ERROR_CAPACITY", 5: "CF_ERROR_NOT_READY", 6: "CF_ERROR_DEVICE_TIMEOUT", 7: "CF_ERROR_BUDGET",
+    8: "CF_ERROR_UNSUPPORTED",
+}
+
+
+class CfError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__("%s (%d): %s" % (STATUS.get(status, "?"), status, message))
+        self.status = status
+
+
+_P = C.c_void_p
+_U32 = C.c_uint32
+_U64 = C.c_uint64
+_PU32 = C.POINTER(C.c_uint32)
+_PU64 = C.POINTER(C.c_uint64)
+_I = C.c_int
+
+# name -> argtypes; every function returns int (CfStatus) unless listed in _RESTYPE
+_SIGS = {
+    "cf_status_string": [_I],
+    "cf_last_error_message": [],
+    "cf_version": [],
+    "cf_context_create": [_I, C.POINTER(_P)],
+    "cf_context_destroy": [_P],
+    "cf_context_check_device_error": [_P, _PU32],
+    "cf_resources_light_create": [_P, C.POINTER(_P)],
+    "cf_resources_light_destroy": [_P],
+    "cf_resources_light_add_lights": [_P, _P, _U32],
+    "cf_resources_light_upload_async": [_P, _P, _U32, _P],
+    "cf_resources_light_update_light_position": [_P, _U32, C.POINTER(C.c_float)],
+    "cf_resources_light_get_light_count": [_P, _PU32],
+    "cf_resources_light_get_device_buffer": [_P, C.POINTER(_P)],
+    "cf_resources_cluster_forward_create": [_P, C.POINTER(_P)],
+    "cf_resources_cluster_forward_destroy": [_P],
+    "cf_resources_cluster_forward_create_buffers": [_P, _U32, _U32, _U32, _U32],
+    "cf_resources_cluster_forward_get_buffers": [_P, C.POINTER(CfClusterForwardBuffers)],
+    "cf_resources_cluster_forward_is_aabb_dirty": [_P, C.POINTER(_I)],
+    "cf_resources_cluster_forward_read_outputs": [_P, _P, _P, _U64, _PU32, _P],
+    "cf_pipeline_aabb_generator_create": [_P, _P, C.POINTER(_P)],
+    "cf_pipeline_aabb_generator_destroy": [_P],
+    "cf_pipeline_aabb_generator_set_cluster_forward_ubo": [_P, C.POINTER(CfClusterForwardUBO)],
+    "cf_pipeline_aabb_generator_on_window_resized": [_P],
+    "cf_pipeline_aabb_generator_fill_command_buffer": [_P, _P],
+    "cf_pipeline_light_culling_create": [_P, _P, _P, C.POINTER(_P)],
+    "cf_pipeline_light_culling_destroy": [_P],
+    "cf_pipeline_light_culling_reset_global_index": [_P],
+    "cf_pipeline_light_culling_set_cluster_forward_ubo": [_P, C.POINTER(CfClusterForwardUBO)],
+    "cf_pipeline_light_culling_fill_command_buffer": [_P, _P],
+    "cf_pipeline_light_culling_set_tuning": [_P, _I, _I, _I, _I],
+    "cf_pipeline_light_culling_enable_stage_timing": [_P, _I],
+    "cf_pipeline_light_culling_get_stage_times": [_P, C.POINTER(C.c_float)],
+    "cf_cull_workspace_size": [_U32, _U32, _U32, _PU64],
+    "cf_generate_aabbs": [C.POINTER(CfClusterForwardUBO), _P, _P],
+    "cf_cull_lights": [C.POINTER(CfClusterForwardUBO), _P, _P, _U32, _U32, _P, _P, _U64, _P, _P, _U64, _P],
+    "cf_cull_workspace_device_error": [_P, _PU32],
+}
+_RESTYPE = {"cf_status_string": C.c_char_p, "cf_last_error_message": C.c_char_p}
+
+_lib = None
+
+
+def declared_symbols():
+    """Names declared with CFCULL_API in include/*.h."""
+    names = []
+    for h in sorted((REPO / "include").glob("*.h")):
+        for m in re.finditer(r"CFCULL_API\s+[\w\s\*]+?\b(cf_\w+)\s*\(", h.read_text()):
+            names.append(m.group(1))
+    return names
+
+
+def lib():
+    """The loaded library; raises if it was not built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(
+                "libcfcull.so is not built (%s); run `python -m hellovulkan_gb300.build` "
+                "or __graft_entry__.build()" % LIB_PATH)
+        L = C.CDLL(str(LIB_PATH))
+        for name, args in _SIGS.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = _RESTYPE.get(name, C.c_int)
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != 0:
+        raise CfError(status, lib().cf_last_error_message().decode(errors="replace"))
+
+
+def ptr(x) -> int | None:
+    """Address of a torch tensor, a numpy array or an int address."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    raise TypeError("cannot take the address of %r" % type(x))
+
+
+def stream_handle(stream) -> int | None:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream

@@ -1,0 +1,77 @@
+// cf_kernels.cuh — launch interface of the clustered-forward CUDA kernels.
+//
+// Data layout in device memory for one view (all 256-byte aligned):
+//   aabbs     C x CfAABB (32 B)            written by the AABB generator, reused
+//                                          while the projection is unchanged
+//   vlights   lpad x float4 (16 B)         view-space light (x, y, z, r^2); lpad is
+//                                          the light count rounded up to 32 and
+//                                          the pad entries are (0, 0, 0, -inf),
+//                                          which fail every test
+//   nonfinite ceil(lpad / 256) x uint32    1 where a 256-light granule holds a
+//                                          light whose view-space position is not
+//                                          finite (those granules take the exact
+//                                          branchy test)
+//   counts    C x uint32                   capped hit count per cluster
+//   staging   C x cap x uint32             each cluster's hits in ascending order
+//   cells     C x CfLightCell              output
+//   indices   >= sum(counts) x uint32      output, packed in cluster order
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cf_types.h"
+
+namespace cfk {
+
+constexpr uint32_t kLightPad = 32;       // view-space light arrays are padded to this
+constexpr uint32_t kFlagGranule = 256;   // lights per non-finite flag word
+constexpr uint32_t kFinalizeChunk = 2048;  // clusters per finalize CTA
+
+// Device error codes (OR-ed into the context's error word).
+constexpr uint32_t kErrFullWaitTimeout = 1u << 0;   // a consumer waited too long for a light tile
+constexpr uint32_t kErrEmptyWaitTimeout = 1u << 1;  // the producer waited too long for a free stage
+
+inline uint32_t pad_lights(uint32_t n) { return (n + kLightPad - 1) / kLightPad * kLightPad; }
+inline uint32_t granules(uint32_t lpad) { return (lpad + kFlagGranule - 1) / kFlagGranule; }
+
+struct ViewCull {
+    const float4* vlights;
+    const uint32_t* nonfinite;
+    const float4* aabbs;
+    uint32_t* counts;
+    uint32_t* staging;
+    CfLightCell* cells;
+    uint32_t* indices;
+    uint32_t* total;  // may be null
+    uint32_t lpad;
+    uint32_t clusters;
+    uint32_t cap;
+    uint32_t pad_;
+};
+
+// One culling configuration: clusters per warp, consumer warps per CTA,
+// lights per shared-memory stage, number of stages.
+struct CullConfig {
+    int clusters_per_warp;
+    int warps;
+    int tile;
+    int stages;
+};
+
+// Workspace carve-up for one view (cf_cull_lights).
+struct WorkspaceLayout {
+    size_t vlights, nonfinite, counts, staging, bytes;
+};
+WorkspaceLayout workspace_layout(uint32_t clusters, uint32_t lights, uint32_t cap);
+
+bool cull_config_supported(const CullConfig& c);
+CullConfig default_cull_config(uint32_t clusters, uint32_t lights);
+
+cudaError_t launch_aabb(const CfClusterForwardUBO& ubo, CfAABB* aabbs, cudaStream_t stream);
+cudaError_t launch_light_xform(const CfLightData* lights, uint32_t count, const float view[16], float4* vlights,
+                               uint32_t* nonfinite, cudaStream_t stream);
+cudaError_t launch_cull(const ViewCull& v, const CullConfig& cfg, uint32_t* dev_error, cudaStream_t stream);
+cudaError_t launch_finalize(const ViewCull& v, cudaStream_t stream);
+
+}  // namespace cfk

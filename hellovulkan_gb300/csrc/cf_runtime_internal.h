@@ -1,0 +1,44 @@
+// cf_runtime_internal.h — helpers shared by the host-side translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cf_kernels.cuh"
+#include "cf_types.h"
+
+namespace cfrt {
+
+constexpr uint32_t kMaxClusters = 1u << 22;  // 4 M clusters per view
+constexpr uint32_t kMaxCap = 4096;           // per-cluster light cap
+constexpr uint32_t kMaxLights = 1u << 26;    // 64 M lights per set
+
+// Records a formatted message for cf_last_error_message() and returns status.
+int fail(int status, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+int cuda_fail(cudaError_t e, const char* what);
+
+bool projection_equal(const CfClusterForwardUBO& a, const CfClusterForwardUBO& b);
+int validate_grid(uint32_t x, uint32_t y, uint32_t z, uint32_t cap, uint32_t* clusters);
+
+// Makes `device` current for the guard's lifetime.
+class DeviceGuard {
+public:
+    explicit DeviceGuard(int device);
+    ~DeviceGuard();
+    cudaError_t err() const { return err_; }
+
+private:
+    int prev_ = -1;
+    cudaError_t err_ = cudaSuccess;
+};
+
+// Ensures *ptr holds at least `bytes` of zero-filled device memory.
+int grow(void** ptr, size_t* capacity, size_t bytes, const char* what);
+
+// Light transform + culling + offset scan of one view on `stream`.
+int enqueue_cull(const CfClusterForwardUBO& ubo, const CfAABB* d_aabbs, const CfLightData* d_lights,
+                 uint32_t light_count, uint32_t cap, CfLightCell* d_cells, uint32_t* d_indices, uint32_t* d_total,
+                 unsigned char* ws, uint32_t* dev_error, const cfk::CullConfig* cfg_override, cudaStream_t stream,
+                 cudaEvent_t* stage_events);
+
+}  // namespace cfrt

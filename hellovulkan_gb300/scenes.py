@@ -1,0 +1,134 @@
+"""Seeded synthetic workloads of the clustered-forward culling path.
+
+No public dataset is involved: every workload is generated here from a seed
+with the shapes, sizes and value distributions of the benchmark
+configurations.
+
+  plain_small    1920x1080, 16x9x24 grid, fovY 45 deg, near 0.1, far 1000,
+                 camera at the origin looking down -Z (identity view);
+                 1024 lights, position U([-20,20]x[0,15]x[-40,10]) (w = 1),
+                 color U[0,1]^3, radius U[1,5]
+  plain_large    2560x1600, 32x18x48 grid, near 0.1, far 2000, camera at
+                 (0,10,60) looking at the origin; 16384 lights from 32
+                 Gaussian blobs (sigma 8) whose centres are uniform in
+                 x in [-100,100], z in [-100,100], height y in [0,30] (y is
+                 up, as in the reference scenes); radius lognormal(ln 3, 0.5)
+                 clipped to [0.5, 20]; cap 150
+  batch_mix      256 views; grid drawn from {8x8x16, 16x9x24, 24x14x32,
+                 32x18x48} with a resolution of matching aspect; light count
+                 log-uniform in [256, 65536], lights as plain_large; camera
+                 uniform in [-80,80]x[2,40]x[-80,80] looking at a uniform
+                 target in [-20,20]^3; near 0.1, far 2000
+
+LightData records are numpy float32 arrays of shape (n, 12): position xyzw,
+color rgba, radius, 3 pad words (the 48-byte std430 record).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .camera import cluster_forward_ubo, look_at_rh
+from ._lib import CfClusterForwardUBO
+
+FOVY = math.radians(45.0)
+GRIDS = ((8, 8, 16), (16, 9, 24), (24, 14, 32), (32, 18, 48))
+# pixel size of a cluster tile for each grid, so that resolution matches aspect
+TILE_PX = {(8, 8, 16): 128, (16, 9, 24): 120, (24, 14, 32): 120, (32, 18, 48): 80}
+CAP = 150
+
+
+@dataclass
+class View:
+    ubo: CfClusterForwardUBO
+    lights: np.ndarray  # (n, 12) float32
+    cap: int = CAP
+    name: str = ""
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def grid(self):
+        return int(self.ubo.sliceCountX), int(self.ubo.sliceCountY), int(self.ubo.sliceCountZ)
+
+    @property
+    def clusters(self) -> int:
+        x, y, z = self.grid
+        return x * y * z
+
+    @property
+    def light_count(self) -> int:
+        return int(self.lights.shape[0])
+
+
+def make_lights(pos: np.ndarray, radius: np.ndarray, color: np.ndarray | None = None) -> np.ndarray:
+    n = pos.shape[0]
+    out = np.zeros((n, 12), np.float32)
+    out[:, 0:3] = pos
+    out[:, 3] = 1.0
+    out[:, 4:7] = color if color is not None else 1.0
+    out[:, 7] = 1.0
+    out[:, 8] = radius
+    return out
+
+
+def uniform_box_lights(rng: np.random.Generator, n: int, lo, hi, rmin=1.0, rmax=5.0) -> np.ndarray:
+    pos = rng.uniform(lo, hi, size=(n, 3)).astype(np.float32)
+    color = rng.uniform(0.0, 1.0, size=(n, 3)).astype(np.float32)
+    radius = rng.uniform(rmin, rmax, size=n).astype(np.float32)
+    return make_lights(pos, radius, color)
+
+
+def blob_lights(rng: np.random.Generator, n: int, n_blobs: int = 32, sigma: float = 8.0) -> np.ndarray:
+    centres = np.stack([rng.uniform(-100, 100, n_blobs), rng.uniform(0, 30, n_blobs),
+                        rng.uniform(-100, 100, n_blobs)], axis=1)
+    which = rng.integers(0, n_blobs, size=n)
+    pos = (centres[which] + rng.normal(0.0, sigma, size=(n, 3))).astype(np.float32)
+    radius = np.clip(rng.lognormal(math.log(3.0), 0.5, size=n), 0.5, 20.0).astype(np.float32)
+    color = rng.uniform(0.0, 1.0, size=(n, 3)).astype(np.float32)
+    return make_lights(pos, radius, color)
+
+
+def plain_small(seed: int = 1, n_lights: int = 1024) -> View:
+    rng = np.random.default_rng(seed)
+    ubo = cluster_forward_ubo(FOVY, 1920, 1080, 0.1, 1000.0, np.eye(4, dtype=np.float32), (16, 9, 24))
+    lights = uniform_box_lights(rng, n_lights, [-20, 0, -40], [20, 15, 10])
+    return View(ubo, lights, CAP, "plain_small 1920x1080 16x9x24 L=%d" % n_lights)
+
+
+def plain_large(seed: int = 2, n_lights: int = 16384, grid=(32, 18, 48)) -> View:
+    rng = np.random.default_rng(seed)
+    view = look_at_rh((0.0, 10.0, 60.0), (0.0, 0.0, 0.0))
+    ubo = cluster_forward_ubo(FOVY, 2560, 1600, 0.1, 2000.0, view, grid)
+    lights = blob_lights(rng, n_lights)
+    return View(ubo, lights, CAP, "plain_large 2560x1600 %dx%dx%d L=%d" % (*grid, n_lights))
+
+
+def random_camera(rng: np.random.Generator):
+    eye = (rng.uniform(-80, 80), rng.uniform(2, 40), rng.uniform(-80, 80))
+    target = tuple(rng.uniform(-20, 20, 3))
+    return look_at_rh(eye, target)
+
+
+def batch_view(rng: np.random.Generator, light_set: np.ndarray | None = None) -> View:
+    grid = GRIDS[int(rng.integers(0, len(GRIDS)))]
+    t = TILE_PX[grid]
+    w, h = grid[0] * t, grid[1] * t
+    ubo = cluster_forward_ubo(FOVY, w, h, 0.1, 2000.0, random_camera(rng), grid)
+    if light_set is None:
+        n = int(round(math.exp(rng.uniform(math.log(256), math.log(65536)))))
+        light_set = blob_lights(rng, n)
+    return View(ubo, light_set, CAP, "batch %dx%dx%d L=%d" % (*grid, light_set.shape[0]))
+
+
+def batch_mix(seed: int = 3, n_views: int = 256) -> list[View]:
+    rng = np.random.default_rng(seed)
+    return [batch_view(rng) for _ in range(n_views)]
+
+
+def custom_view(grid, width, height, near, far, view=None, lights=None, cap=CAP, fovy=FOVY) -> View:
+    view = np.eye(4, dtype=np.float32) if view is None else view
+    ubo = cluster_forward_ubo(fovy, width, height, near, far, view, grid)
+    lights = np.zeros((0, 12), np.float32) if lights is None else lights
+    return View(ubo, lights, cap, "custom")

@@ -1,0 +1,106 @@
+/*
+ * cf_types.h — buffer records shared by the clustered-forward light-culling
+ * library, its kernels and its host callers.
+ *
+ * Every record is byte-identical to the record the HelloVulkan clustered
+ * forward pipeline already binds, so an engine hands its own buffers (or
+ * copies of them) to this library without repacking:
+ *
+ *   CfLightData          <-> LightData         Shaders/LightData.glsl:1-6 (std430,
+ *                                              array stride 48) and
+ *                                              Header/Resources/ResourcesLight.h:13-21
+ *   CfAABB               <-> AABB              Shaders/AABB/AABB.glsl:1-5,
+ *                                              Header/Resources/ResourcesLight.h:24-30
+ *   CfLightCell          <-> LightCell         Shaders/ClusteredForward/Header.glsl:1-5,
+ *                                              Header/Resources/ResourcesLight.h:33-39
+ *   CfClusterForwardUBO  <-> ClusterForwardUBO Shaders/ClusteredForward/Header.glsl:7-19
+ *                                              (std140), Header/UBOs.h:67-89 (C++ sizeof 176)
+ *
+ * Matrices are column-major, element (col, row) at [col * 4 + row], as GLSL
+ * and glm store them.
+ *
+ * Plain C99 / C++ / CUDA; no dependencies beyond <stdint.h>.
+ */
+#ifndef CF_TYPES_H
+#define CF_TYPES_H
+
+#include <stdint.h>
+
+#if defined(__cplusplus)
+#define CF_ALIGNAS(n) alignas(n)
+#else
+#define CF_ALIGNAS(n) _Alignas(n)
+#endif
+
+/* Per-cluster light cap of the reference (Header/Configs.h:55,
+ * Shaders/ClusteredForward/LightCulling.comp:17). */
+#define CF_MAX_LIGHTS_PER_CLUSTER_DEFAULT 150u
+
+/* Default grid of the reference (Header/Configs.h:49-52). */
+#define CF_SLICE_COUNT_X_DEFAULT 16u
+#define CF_SLICE_COUNT_Y_DEFAULT 9u
+#define CF_SLICE_COUNT_Z_DEFAULT 24u
+
+/* One point light, std430 array element: position (w = 1) @0, color @16,
+ * radius @32, padded to a 48-byte stride. */
+typedef struct CfLightData {
+    CF_ALIGNAS(16) float position[4];
+    float color[4];
+    float radius;
+    float _pad[3];
+} CfLightData;
+
+/* One cluster's view-space bounding box; w is 0 in both points. */
+typedef struct CfAABB {
+    CF_ALIGNAS(16) float minPoint[4];
+    float maxPoint[4];
+} CfAABB;
+
+/* Where a cluster's light indices live in the index list. */
+typedef struct CfLightCell {
+    uint32_t offset;
+    uint32_t count;
+} CfLightCell;
+
+/* Per-view parameters, std140: invProj @0, view @64, screenSize @128,
+ * sliceScaling @136, sliceBias @140, near @144, far @148, X/Y/Z @152/156/160.
+ * 164 bytes are used; the C++ mirror in the reference is 176 bytes. */
+typedef struct CfClusterForwardUBO {
+    CF_ALIGNAS(16) float cameraInverseProjection[16];
+    float cameraView[16];
+    float screenSize[2];
+    float sliceScaling;
+    float sliceBias;
+    float cameraNear;
+    float cameraFar;
+    uint32_t sliceCountX;
+    uint32_t sliceCountY;
+    uint32_t sliceCountZ;
+    uint32_t _pad[3];
+} CfClusterForwardUBO;
+
+#if defined(__cplusplus)
+#include <cstddef>
+static_assert(alignof(CfLightData) == 16 && alignof(CfAABB) == 16 && alignof(CfClusterForwardUBO) == 16,
+              "16-byte aligned records");
+static_assert(sizeof(CfLightData) == 48, "LightData std430 stride is 48");
+static_assert(offsetof(CfLightData, position) == 0, "LightData.position @0");
+static_assert(offsetof(CfLightData, color) == 16, "LightData.color @16");
+static_assert(offsetof(CfLightData, radius) == 32, "LightData.radius @32");
+static_assert(sizeof(CfAABB) == 32, "AABB is two vec4");
+static_assert(offsetof(CfAABB, maxPoint) == 16, "AABB.maxPoint @16");
+static_assert(sizeof(CfLightCell) == 8, "LightCell is two uint");
+static_assert(offsetof(CfLightCell, count) == 4, "LightCell.count @4");
+static_assert(sizeof(CfClusterForwardUBO) == 176, "ClusterForwardUBO C++ sizeof");
+static_assert(offsetof(CfClusterForwardUBO, cameraView) == 64, "view @64");
+static_assert(offsetof(CfClusterForwardUBO, screenSize) == 128, "screenSize @128");
+static_assert(offsetof(CfClusterForwardUBO, sliceScaling) == 136, "sliceScaling @136");
+static_assert(offsetof(CfClusterForwardUBO, sliceBias) == 140, "sliceBias @140");
+static_assert(offsetof(CfClusterForwardUBO, cameraNear) == 144, "near @144");
+static_assert(offsetof(CfClusterForwardUBO, cameraFar) == 148, "far @148");
+static_assert(offsetof(CfClusterForwardUBO, sliceCountX) == 152, "X @152");
+static_assert(offsetof(CfClusterForwardUBO, sliceCountY) == 156, "Y @156");
+static_assert(offsetof(CfClusterForwardUBO, sliceCountZ) == 160, "Z @160");
+#endif
+
+#endif /* CF_TYPES_H */

@@ -1,0 +1,217 @@
+/*
+ * cfcull.h — C ABI of the GB300 clustered-forward light-culling library.
+ *
+ * The library replaces the two compute passes of HelloVulkan's clustered
+ * forward renderer — the cluster AABB generator and the light culling pass —
+ * with CUDA kernels for sm_103a.  Its objects mirror the reference's plugin
+ * classes one to one, so a host that drove
+ *
+ *     ResourcesLight, ResourcesClusterForward,
+ *     PipelineAABBGenerator, PipelineLightCulling
+ *
+ * drives the same calls here (each declaration cites the member it
+ * replaces).  Buffers keep the reference layouts (cf_types.h), so the
+ * LightCell list and the light-index list feed the unchanged cluster-forward
+ * fragment shader (Shaders/ClusteredForward/Scene.frag:64-78,119-134).
+ *
+ * Conventions
+ *  - Every function returns a CfStatus (0 = success) and never throws.
+ *    cf_last_error_message() gives a human-readable detail of the last failure
+ *    on the calling thread.
+ *  - `stream` arguments are cudaStream_t passed as void* (NULL = the legacy
+ *    default stream).  Work is enqueued asynchronously unless stated.
+ *  - Handles are not thread-safe; use one per thread or serialise.
+ *  - The caller owns host memory; the library owns the device memory of its
+ *    objects.  Device pointers returned by *_get_* stay valid until the
+ *    object is destroyed or its buffers are re-created.
+ *  - Light indices are 32-bit and view-local; the index list is packed in
+ *    cluster order: cell c's indices start at the exclusive prefix sum of the
+ *    counts of clusters 0..c-1.  The reference reserves the same slices with
+ *    a global atomicAdd (LightCulling.comp:79), which gives the same cells
+ *    and list when its workgroups run in index order and a permutation of the
+ *    slices otherwise; each cluster's own list is identical in both cases:
+ *    the first max_lights_per_cluster hits in ascending light order.
+ */
+#ifndef CFCULL_H
+#define CFCULL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "cf_types.h"
+
+#if defined(__GNUC__)
+#define CFCULL_API __attribute__((visibility("default")))
+#else
+#define CFCULL_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum CfStatus {
+    CF_SUCCESS = 0,
+    CF_ERROR_INVALID_ARGUMENT = 1, /* null handle/pointer, zero or oversized grid, cap 0, ... */
+    CF_ERROR_OUT_OF_MEMORY = 2,    /* a device or pinned allocation failed                  */
+    CF_ERROR_CUDA = 3,             /* a CUDA runtime call failed (see the message)          */
+    CF_ERROR_CAPACITY = 4,         /* an output or workspace buffer is too small            */
+    CF_ERROR_NOT_READY = 5,        /* a required input (UBO, lights, buffers) was never set */
+    CF_ERROR_DEVICE_TIMEOUT = 6,   /* a bounded wait inside a kernel gave up                */
+    CF_ERROR_BUDGET = 7,           /* an admission would exceed the device-memory budget    */
+    CF_ERROR_UNSUPPORTED = 8,      /* no usable sm_103 device                              */
+} CfStatus;
+
+CFCULL_API const char* cf_status_string(int status);
+/* Detail of the most recent failing call on this thread ("" if none). */
+CFCULL_API const char* cf_last_error_message(void);
+/* Library version as 10000*major + 100*minor + patch. */
+CFCULL_API int cf_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Context: one CUDA device (stands in for VulkanContext).                  */
+/* ------------------------------------------------------------------------ */
+typedef struct CfContext CfContext;
+
+CFCULL_API int cf_context_create(int device, CfContext** out);
+CFCULL_API int cf_context_destroy(CfContext* ctx);
+/* Reads and clears the device-side error word that bounded in-kernel waits
+ * set on timeout (0 = none).  Synchronises the device. */
+CFCULL_API int cf_context_check_device_error(CfContext* ctx, uint32_t* device_error);
+
+/* ------------------------------------------------------------------------ */
+/* ResourcesLight — Header/Resources/ResourcesLight.h:42-81                  */
+/* ------------------------------------------------------------------------ */
+typedef struct CfResourcesLight CfResourcesLight;
+
+CFCULL_API int cf_resources_light_create(CfContext* ctx, CfResourcesLight** out);
+CFCULL_API int cf_resources_light_destroy(CfResourcesLight* res);
+/* ResourcesLight::AddLights (Source/Resources/ResourcesLight.cpp:8-18):
+ * replaces the light set with `count` records and uploads them.  Synchronous. */
+CFCULL_API int cf_resources_light_add_lights(CfResourcesLight* res, const CfLightData* lights, uint32_t count);
+/* Asynchronous upload into the existing device buffer (grown if needed,
+ * which synchronises).  `lights` should be pinned for a truly async copy. */
+CFCULL_API int cf_resources_light_upload_async(CfResourcesLight* res, const CfLightData* lights, uint32_t count,
+                                               void* stream);
+/* ResourcesLight::UpdateLightPosition (Source/Resources/ResourcesLight.cpp:20-29):
+ * sets light `index` to (x, y, z, 1).  Out-of-range indices are ignored, as
+ * in the reference.  Synchronous. */
+CFCULL_API int cf_resources_light_update_light_position(CfResourcesLight* res, uint32_t index, const float position[3]);
+/* ResourcesLight::GetLightCount */
+CFCULL_API int cf_resources_light_get_light_count(const CfResourcesLight* res, uint32_t* count);
+/* ResourcesLight::GetVulkanBufferPtr: device pointer to the CfLightData array. */
+CFCULL_API int cf_resources_light_get_device_buffer(const CfResourcesLight* res, const CfLightData** device_lights);
+
+/* ------------------------------------------------------------------------ */
+/* ResourcesClusterForward — Header/Resources/ResourcesClusterForward.h:11-31 */
+/* ------------------------------------------------------------------------ */
+typedef struct CfResourcesClusterForward CfResourcesClusterForward;
+
+typedef struct CfClusterForwardBuffers {
+    CfAABB* aabbs;            /* aabbBuffer_:         cluster_count records       */
+    CfLightCell* light_cells; /* lightCellsBuffer_:   cluster_count records       */
+    uint32_t* light_indices;  /* lightIndicesBuffer_: index_capacity entries      */
+    uint32_t* total_indices;  /* one uint32: indices written by the last culling  */
+    uint32_t cluster_count;
+    uint32_t max_lights_per_cluster;
+    uint64_t index_capacity;  /* = cluster_count * max_lights_per_cluster         */
+} CfClusterForwardBuffers;
+
+CFCULL_API int cf_resources_cluster_forward_create(CfContext* ctx, CfResourcesClusterForward** out);
+CFCULL_API int cf_resources_cluster_forward_destroy(CfResourcesClusterForward* res);
+/* ResourcesClusterForward::CreateBuffers (Source/Resources/ResourcesClusterForward.cpp:5-34)
+ * with the grid and cap as arguments instead of compile-time constants
+ * (the reference uses 16 x 9 x 24 and 150).  Marks the AABBs dirty. */
+CFCULL_API int cf_resources_cluster_forward_create_buffers(CfResourcesClusterForward* res, uint32_t slice_count_x,
+                                                           uint32_t slice_count_y, uint32_t slice_count_z,
+                                                           uint32_t max_lights_per_cluster);
+CFCULL_API int cf_resources_cluster_forward_get_buffers(const CfResourcesClusterForward* res,
+                                                        CfClusterForwardBuffers* out);
+/* ResourcesClusterForward::aabbDirty_ */
+CFCULL_API int cf_resources_cluster_forward_is_aabb_dirty(const CfResourcesClusterForward* res, int* dirty);
+/* Copies the cells and the first min(total, host_index_capacity) indices to
+ * host memory and returns the total; synchronises `stream`. */
+CFCULL_API int cf_resources_cluster_forward_read_outputs(CfResourcesClusterForward* res, CfLightCell* host_cells,
+                                                         uint32_t* host_indices, uint64_t host_index_capacity,
+                                                         uint32_t* total, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* PipelineAABBGenerator — Header/Pipelines/PipelineAABBGenerator.h:17-39    */
+/* ------------------------------------------------------------------------ */
+typedef struct CfPipelineAABBGenerator CfPipelineAABBGenerator;
+
+CFCULL_API int cf_pipeline_aabb_generator_create(CfContext* ctx, CfResourcesClusterForward* res_cf,
+                                                 CfPipelineAABBGenerator** out);
+CFCULL_API int cf_pipeline_aabb_generator_destroy(CfPipelineAABBGenerator* pipe);
+/* PipelineAABBGenerator::SetClusterForwardUBO.  A UBO whose projection part
+ * (inverse projection, near, far, grid) differs from the one the AABBs were
+ * built from marks the AABBs dirty, so zoom changes also regenerate them. */
+CFCULL_API int cf_pipeline_aabb_generator_set_cluster_forward_ubo(CfPipelineAABBGenerator* pipe,
+                                                                  const CfClusterForwardUBO* ubo);
+/* PipelineAABBGenerator::OnWindowResized (PipelineAABBGenerator.cpp:31-34) */
+CFCULL_API int cf_pipeline_aabb_generator_on_window_resized(CfPipelineAABBGenerator* pipe);
+/* PipelineAABBGenerator::FillCommandBuffer (PipelineAABBGenerator.cpp:36-47):
+ * enqueues the generator on `stream` when the AABBs are dirty, else nothing. */
+CFCULL_API int cf_pipeline_aabb_generator_fill_command_buffer(CfPipelineAABBGenerator* pipe, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* PipelineLightCulling — Header/Pipelines/PipelineLightCulling.h:18-30      */
+/* ------------------------------------------------------------------------ */
+typedef struct CfPipelineLightCulling CfPipelineLightCulling;
+
+CFCULL_API int cf_pipeline_light_culling_create(CfContext* ctx, CfResourcesLight* res_light,
+                                                CfResourcesClusterForward* res_cf, CfPipelineLightCulling** out);
+CFCULL_API int cf_pipeline_light_culling_destroy(CfPipelineLightCulling* pipe);
+/* PipelineLightCulling::ResetGlobalIndex (PipelineLightCulling.cpp:38-43).
+ * Kept for call compatibility; offsets come from a prefix scan, so there is
+ * no counter to reset and this does nothing. */
+CFCULL_API int cf_pipeline_light_culling_reset_global_index(CfPipelineLightCulling* pipe);
+/* PipelineLightCulling::SetClusterForwardUBO (PipelineLightCulling.cpp:45-49) */
+CFCULL_API int cf_pipeline_light_culling_set_cluster_forward_ubo(CfPipelineLightCulling* pipe,
+                                                                 const CfClusterForwardUBO* ubo);
+/* PipelineLightCulling::FillCommandBuffer (PipelineLightCulling.cpp:51-119):
+ * enqueues light transform, culling and the offset scan on `stream`. */
+CFCULL_API int cf_pipeline_light_culling_fill_command_buffer(CfPipelineLightCulling* pipe, void* stream);
+
+/* Tuning: selects the culling kernel configuration (clusters per warp,
+ * consumer warps per CTA, lights per shared-memory stage, stages); all zero
+ * restores the automatic choice.  Unsupported combinations are rejected. */
+CFCULL_API int cf_pipeline_light_culling_set_tuning(CfPipelineLightCulling* pipe, int clusters_per_warp, int warps,
+                                                    int tile, int stages);
+/* Stage timing, the counterpart of the reference's Tracy GPU zone
+ * "Light_Culling" (PipelineLightCulling.cpp:53): when enabled, each
+ * fill_command_buffer records CUDA events around its three kernels, and
+ * get_stage_times returns the last call's light-transform, culling and
+ * offset-scan durations in milliseconds (waits for them). */
+CFCULL_API int cf_pipeline_light_culling_enable_stage_timing(CfPipelineLightCulling* pipe, int enable);
+CFCULL_API int cf_pipeline_light_culling_get_stage_times(CfPipelineLightCulling* pipe, float ms[3]);
+
+/* ------------------------------------------------------------------------ */
+/* Stateless entry points on caller-owned device memory.                     */
+/* ------------------------------------------------------------------------ */
+
+/* Bytes of device workspace cf_cull_lights needs. */
+CFCULL_API int cf_cull_workspace_size(uint32_t cluster_count, uint32_t light_count, uint32_t max_lights_per_cluster,
+                                      uint64_t* bytes);
+/* AABBGenerator.comp over the grid of `ubo` (host pointer) into
+ * d_aabbs[X*Y*Z] (device). */
+CFCULL_API int cf_generate_aabbs(const CfClusterForwardUBO* ubo, CfAABB* d_aabbs, void* stream);
+/* LightCulling.comp: d_cells[C] and d_indices (capacity >= C * cap) from
+ * d_aabbs[C] and d_lights[light_count]; d_total (optional, device) receives
+ * the number of indices.  d_workspace: >= cf_cull_workspace_size bytes,
+ * 256-byte aligned, zero-filled once after allocation (its first word is the
+ * device error word that bounded in-kernel waits set on timeout). */
+CFCULL_API int cf_cull_lights(const CfClusterForwardUBO* ubo, const CfAABB* d_aabbs, const CfLightData* d_lights,
+                              uint32_t light_count, uint32_t max_lights_per_cluster, CfLightCell* d_cells,
+                              uint32_t* d_indices, uint64_t index_capacity, uint32_t* d_total, void* d_workspace,
+                              uint64_t workspace_bytes, void* stream);
+
+/* Reads and clears the device error word of a cf_cull_lights workspace
+ * (0 = none; CF_ERROR_DEVICE_TIMEOUT otherwise).  Synchronises the device. */
+CFCULL_API int cf_cull_workspace_device_error(void* d_workspace, uint32_t* device_error);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CFCULL_H */

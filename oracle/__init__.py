@@ -1,0 +1,122 @@
+"""Python access to the CPU oracle and to the reference shaders compiled as C++.
+
+TEST INFRASTRUCTURE ONLY: imported by the tests, by ``__graft_entry__.smoke()``
+and by the CPU-baseline leg of ``bench.py``, as the checker of the CUDA path.
+
+* ``Oracle`` wraps ``oracle/_build/libcf_oracle.so`` (cf_oracle.cpp, the
+  restatement of AABBGenerator.comp and LightCulling.comp).
+* ``Reference`` wraps ``oracle/_ref/libcf_ref.so``: the reference's own two
+  shaders compiled as C++ (see oracle/build.py); available only where their
+  generated translation unit exists.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+_P = C.c_void_p
+
+
+def _ubo_ptr(ubo):
+    return C.byref(ubo)
+
+
+class Oracle:
+    def __init__(self, path: Path | None = None):
+        path = path or _build.build_oracle()
+        L = C.CDLL(str(path))
+        L.cfo_generate_aabbs.argtypes = [_P, _P, C.c_int]
+        L.cfo_cull.argtypes = [_P, _P, _P, C.c_uint32, C.c_uint32, _P, _P, C.c_uint64,
+                               C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.c_int]
+        for f in ("cfo_pow", "cfo_log2", "cfo_exp2"):
+            getattr(L, f).restype = C.c_float
+        L.cfo_pow.argtypes = [C.c_float, C.c_float]
+        L.cfo_log2.argtypes = [C.c_float]
+        L.cfo_exp2.argtypes = [C.c_float]
+        L.cfo_fp_contract_probe.argtypes = []
+        L.cfo_max_threads.argtypes = []
+        self.lib = L
+
+    def generate_aabbs(self, ubo, threads: int = 0) -> np.ndarray:
+        C_ = int(ubo.sliceCountX) * int(ubo.sliceCountY) * int(ubo.sliceCountZ)
+        out = np.empty((C_, 8), np.float32)
+        st = self.lib.cfo_generate_aabbs(_ubo_ptr(ubo), out.ctypes.data, threads)
+        assert st == 0, st
+        return out
+
+    def cull(self, ubo, aabbs: np.ndarray, lights: np.ndarray, cap: int = 150, threads: int = 0):
+        """Returns (cells (C,2) uint32, indices (total,) uint32, executed_tests)."""
+        C_ = int(ubo.sliceCountX) * int(ubo.sliceCountY) * int(ubo.sliceCountZ)
+        aabbs = np.ascontiguousarray(aabbs, np.float32)
+        lights = np.ascontiguousarray(lights, np.float32).reshape(-1, 12)
+        cells = np.empty((C_, 2), np.uint32)
+        cap_total = C_ * cap
+        idx = np.empty(max(cap_total, 1), np.uint32)
+        total = C.c_uint64()
+        executed = C.c_uint64()
+        st = self.lib.cfo_cull(_ubo_ptr(ubo), aabbs.ctypes.data, lights.ctypes.data if lights.size else None,
+                               lights.shape[0], cap, cells.ctypes.data, idx.ctypes.data, cap_total,
+                               C.byref(total), C.byref(executed), threads)
+        assert st == 0, st
+        return cells, idx[: total.value].copy(), int(executed.value)
+
+    def pow(self, x: float, y: float) -> float:
+        return self.lib.cfo_pow(x, y)
+
+    def log2(self, x: float) -> float:
+        return self.lib.cfo_log2(x)
+
+    def exp2(self, x: float) -> float:
+        return self.lib.cfo_exp2(x)
+
+    def fp_contract_probe(self) -> int:
+        return self.lib.cfo_fp_contract_probe()
+
+    def max_threads(self) -> int:
+        return self.lib.cfo_max_threads()
+
+
+class Reference:
+    """The reference's AABBGenerator.comp / LightCulling.comp run on the CPU."""
+
+    def __init__(self, path: Path):
+        L = C.CDLL(str(path))
+        L.cfr_generate_aabbs.argtypes = [_P, _P, C.c_int]
+        L.cfr_cull.argtypes = [_P, _P, _P, C.c_uint32, _P, _P, C.c_uint64, C.POINTER(C.c_uint32), C.c_int]
+        L.cfr_max_lights_per_cluster.restype = C.c_uint32
+        self.lib = L
+        self.cap = int(L.cfr_max_lights_per_cluster())
+
+    @classmethod
+    def load(cls):
+        """The reference library, or None where it cannot be built."""
+        try:
+            p = _build.build_ref()
+        except Exception:
+            return None
+        return cls(p) if p else None
+
+    def generate_aabbs(self, ubo, threads: int = 1) -> np.ndarray:
+        C_ = int(ubo.sliceCountX) * int(ubo.sliceCountY) * int(ubo.sliceCountZ)
+        out = np.empty((C_, 8), np.float32)
+        assert self.lib.cfr_generate_aabbs(_ubo_ptr(ubo), out.ctypes.data, threads) == 0
+        return out
+
+    def cull(self, ubo, aabbs: np.ndarray, lights: np.ndarray, threads: int = 1):
+        """Returns (cells (C,2) uint32, indices (total,) uint32); threads=1 runs
+        the workgroups in index order, so offsets are the cluster-order scan."""
+        C_ = int(ubo.sliceCountX) * int(ubo.sliceCountY) * int(ubo.sliceCountZ)
+        aabbs = np.ascontiguousarray(aabbs, np.float32)
+        lights = np.ascontiguousarray(lights, np.float32).reshape(-1, 12)
+        cells = np.empty((C_, 2), np.uint32)
+        cap_total = C_ * self.cap
+        idx = np.zeros(max(cap_total, 1), np.uint32)
+        total = C.c_uint32()
+        st = self.lib.cfr_cull(_ubo_ptr(ubo), aabbs.ctypes.data, lights.ctypes.data if lights.size else None,
+                               lights.shape[0], cells.ctypes.data, idx.ctypes.data, cap_total, C.byref(total), threads)
+        assert st == 0, st
+        return cells, idx[: total.value].copy()

@@ -1,0 +1,209 @@
+/*
+ * cf_oracle.cpp — CPU oracle for the clustered-forward light-culling path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Only the tests, the smoke check and the CPU
+ * baseline leg of the benchmark load this library, always as the checker of
+ * the CUDA path and never as a part of it.
+ *
+ * A scalar restatement of the two compute shaders of HelloVulkan's clustered
+ * forward pass, in the shaders' own operation order:
+ *
+ *   cfo_generate_aabbs  HelloVulkan/Shaders/ClusteredForward/AABBGenerator.comp:18-89
+ *   cfo_cull            HelloVulkan/Shaders/ClusteredForward/LightCulling.comp:26-87
+ *
+ * with the three implementation-defined parts of GLSL pinned exactly as in
+ * include/cf_pinned_math.h (pow, mat4*vec4 summation order, no FMA).  This
+ * file restates the mat4*vec4 order and the GLSL min/max with its own code
+ * and takes only pow from that header, because pow has no unique value.
+ *
+ * The reference reserves each cluster's slice of the index list with an
+ * atomicAdd on a global counter (LightCulling.comp:79), so its offsets depend
+ * on scheduling.  The oracle assigns offsets by an exclusive scan of the
+ * per-cluster counts in cluster-index order, which is what the reference
+ * produces when its workgroups run one after another in index order.
+ *
+ * Build: oracle/build.py (g++ -O2 -ffp-contract=off, OpenMP over clusters).
+ */
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <omp.h>
+
+#include "cf_types.h"
+#include "cf_pinned_math.h"
+
+namespace {
+
+struct V3 { float x, y, z; };
+struct V4 { float x, y, z, w; };
+
+/* GLSL M * v, column-major M, summed left to right (no FMA: -ffp-contract=off). */
+inline V4 mat_mul(const float* m, const V4& v)
+{
+    V4 r;
+    r.x = ((m[0] * v.x + m[4] * v.y) + m[8] * v.z) + m[12] * v.w;
+    r.y = ((m[1] * v.x + m[5] * v.y) + m[9] * v.z) + m[13] * v.w;
+    r.z = ((m[2] * v.x + m[6] * v.y) + m[10] * v.z) + m[14] * v.w;
+    r.w = ((m[3] * v.x + m[7] * v.y) + m[11] * v.z) + m[15] * v.w;
+    return r;
+}
+
+inline float gmin(float x, float y) { return (y < x) ? y : x; }
+inline float gmax(float x, float y) { return (x < y) ? y : x; }
+inline V3 gmin3(const V3& a, const V3& b) { return {gmin(a.x, b.x), gmin(a.y, b.y), gmin(a.z, b.z)}; }
+inline V3 gmax3(const V3& a, const V3& b) { return {gmax(a.x, b.x), gmax(a.y, b.y), gmax(a.z, b.z)}; }
+
+/* AABBGenerator.comp:18-32 */
+inline V4 screen_to_view(const CfClusterForwardUBO& u, const V4& screen)
+{
+    const V4 clip = {screen.x * 2.0f - 1.0f, screen.y * 2.0f - 1.0f, screen.z, screen.w};
+    V4 view = mat_mul(u.cameraInverseProjection, clip);
+    const float w = view.w;
+    view.x = view.x / w;
+    view.y = view.y / w;
+    view.z = view.z / w;
+    view.w = view.w / w;
+    return view;
+}
+
+/* AABBGenerator.comp:34-37: (incident * zOffset) / incident.z */
+inline V3 ray_intersect_z_plane(const V3& incident, float z_offset)
+{
+    return {(incident.x * z_offset) / incident.z,
+            (incident.y * z_offset) / incident.z,
+            (incident.z * z_offset) / incident.z};
+}
+
+/* AABBGenerator.comp:39-89 for workgroup (i, j, k). */
+inline void aabb_one(const CfClusterForwardUBO& u, uint32_t i, uint32_t j, uint32_t k, CfAABB* out)
+{
+    const float npx = 1.0f / float(u.sliceCountX);
+    const float npy = 1.0f / float(u.sliceCountY);
+    const V4 max_ss = {(float(i) + 1.0f) * npx, (float(j) + 1.0f) * npy, 0.0f, 1.0f};
+    const V4 min_ss = {float(i) * npx, float(j) * npy, 0.0f, 1.0f};
+    const V4 mx = screen_to_view(u, max_ss);
+    const V4 mn = screen_to_view(u, min_ss);
+    const V3 max_vs = {mx.x, mx.y, mx.z};
+    const V3 min_vs = {mn.x, mn.y, mn.z};
+    const float ratio = u.cameraFar / u.cameraNear;
+    const float tile_near = -u.cameraNear * cf_pow_pinned(ratio, float(k) / float(u.sliceCountZ));
+    const float tile_far = -u.cameraNear * cf_pow_pinned(ratio, float(k + 1u) / float(u.sliceCountZ));
+    const V3 min_near = ray_intersect_z_plane(min_vs, tile_near);
+    const V3 min_far = ray_intersect_z_plane(min_vs, tile_far);
+    const V3 max_near = ray_intersect_z_plane(max_vs, tile_near);
+    const V3 max_far = ray_intersect_z_plane(max_vs, tile_far);
+    const V3 lo = gmin3(gmin3(min_near, min_far), gmin3(max_near, max_far));
+    const V3 hi = gmax3(gmax3(min_near, min_far), gmax3(max_near, max_far));
+    out->minPoint[0] = lo.x; out->minPoint[1] = lo.y; out->minPoint[2] = lo.z; out->minPoint[3] = 0.0f;
+    out->maxPoint[0] = hi.x; out->maxPoint[1] = hi.y; out->maxPoint[2] = hi.z; out->maxPoint[3] = 0.0f;
+}
+
+/* LightCulling.comp:26-47 */
+inline float sq_dist_point_aabb(const float p[3], const CfAABB& cell)
+{
+    float sq = 0.0f;
+    for (int a = 0; a < 3; ++a) {
+        const float v = p[a];
+        if (v < cell.minPoint[a]) {
+            const float d = cell.minPoint[a] - v;
+            sq += d * d;
+        } else if (v > cell.maxPoint[a]) {
+            const float d = cell.maxPoint[a] - v;
+            sq += d * d;
+        }
+    }
+    return sq;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cfo_generate_aabbs(const CfClusterForwardUBO* ubo, CfAABB* out, int threads)
+{
+    if (!ubo || !out) return 1;
+    const uint32_t X = ubo->sliceCountX, Y = ubo->sliceCountY, Z = ubo->sliceCountZ;
+    const int64_t C = int64_t(X) * Y * Z;
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int64_t c = 0; c < C; ++c) {
+        const uint32_t i = uint32_t(c % X), j = uint32_t((c / X) % Y), k = uint32_t(c / (int64_t(X) * Y));
+        aabb_one(*ubo, i, j, k, out + c);
+    }
+    return 0;
+}
+
+/*
+ * LightCulling.comp:59-87 for every cluster.  Writes cells[C] and the packed
+ * index list; *total_out = number of indices written.  *executed_tests_out =
+ * sum over clusters of the number of TestSphereAABB calls the reference loop
+ * makes (it stops after the cap-th hit).  Returns 0, 1 (bad argument) or
+ * 2 (index_capacity too small).
+ */
+int cfo_cull(const CfClusterForwardUBO* ubo, const CfAABB* aabbs, const CfLightData* lights,
+             uint32_t light_count, uint32_t cap, CfLightCell* cells, uint32_t* indices,
+             uint64_t index_capacity, uint64_t* total_out, uint64_t* executed_tests_out,
+             int threads)
+{
+    if (!ubo || !aabbs || !cells || cap == 0 || (light_count && !lights)) return 1;
+    const int64_t C = int64_t(ubo->sliceCountX) * ubo->sliceCountY * ubo->sliceCountZ;
+    if (threads <= 0) threads = omp_get_max_threads();
+    std::vector<uint32_t> stage(static_cast<size_t>(C) * cap);
+    std::vector<uint32_t> count(static_cast<size_t>(C));
+    uint64_t executed = 0;
+    const float* V = ubo->cameraView;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 8) reduction(+ : executed)
+    for (int64_t c = 0; c < C; ++c) {
+        const CfAABB cell = aabbs[c];
+        uint32_t* mine = stage.data() + size_t(c) * cap;
+        uint32_t n = 0;
+        uint32_t i = 0;
+        for (; i < light_count && n < cap; ++i) {
+            const CfLightData& L = lights[i];
+            const V4 pw = {L.position[0], L.position[1], L.position[2], L.position[3]};
+            const V4 pv = mat_mul(V, pw);
+            const float p[3] = {pv.x, pv.y, pv.z};
+            const float sq = sq_dist_point_aabb(p, cell);
+            if (sq < L.radius * L.radius) mine[n++] = i;
+        }
+        executed += i;
+        count[size_t(c)] = n;
+    }
+    uint64_t off = 0;
+    for (int64_t c = 0; c < C; ++c) {
+        cells[c].offset = uint32_t(off);
+        cells[c].count = count[size_t(c)];
+        off += count[size_t(c)];
+    }
+    if (total_out) *total_out = off;
+    if (executed_tests_out) *executed_tests_out = executed;
+    if (off > index_capacity) return 2;
+    if (off && !indices) return 1;
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int64_t c = 0; c < C; ++c) {
+        if (cells[c].count)
+            memcpy(indices + cells[c].offset, stage.data() + size_t(c) * cap, sizeof(uint32_t) * cells[c].count);
+    }
+    return 0;
+}
+
+float cfo_pow(float x, float y) { return cf_pow_pinned(x, y); }
+float cfo_log2(float x) { return cf_log2_pinned(x); }
+float cfo_exp2(float x) { return cf_exp2_pinned(x); }
+
+/* 1 when a*b+c is evaluated with two roundings (no contraction), else 0. */
+int cfo_fp_contract_probe(void)
+{
+    /* (1 + 2^-12)^2 = 1 + 2^-11 + 2^-24 rounds (tie to even) to 1 + 2^-11, so
+     * the unfused sum is 0 and a fused one keeps 2^-24. */
+    volatile float va = 1.0f + 0x1p-12f, vc = -(1.0f + 0x1p-11f);
+    const float a = va, b = va, c = vc;
+    const float r = a * b + c;
+    if (r == 0.0f) return 1;
+    if (r == 0x1p-24f) return 0;
+    return -1;
+}
+
+int cfo_max_threads(void) { return omp_get_max_threads(); }
+
+}  // extern "C"

@@ -1,0 +1,171 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle and the
+golden fixtures made from the reference's own shaders.  The bar is bit-exact:
+AABB float bits, LightCells and the index list."""
+import numpy as np
+import pytest
+
+from gpu_helpers import assert_matches_oracle, bits, run_pipeline, run_stateless, sha
+from hellovulkan_gb300 import scenes
+from hellovulkan_gb300.camera import look_at_rh, ubo_from_bytes
+
+pytestmark = pytest.mark.gpu
+
+TUNINGS = [(1, 4, 512, 4), (2, 4, 512, 4), (4, 4, 512, 4), (1, 8, 512, 4), (2, 8, 512, 4), (4, 8, 512, 4)]
+
+
+def golden_views(golden):
+    for name in [str(n) for n in golden["names"]]:
+        v = scenes.View(ubo_from_bytes(golden[name + "/ubo"]), golden[name + "/lights"],
+                        int(golden[name + "/cap"][0]), name)
+        yield name, v
+
+
+def test_golden_cases_through_the_pipelines(gpu, golden):
+    for name, v in golden_views(golden):
+        aabbs, cells, idx = run_pipeline(gpu, v)
+        if name + "/aabbs" in golden.files:
+            assert np.array_equal(bits(aabbs), golden[name + "/aabbs"]), name
+            assert np.array_equal(cells, golden[name + "/cells"]), name
+            assert np.array_equal(idx, golden[name + "/indices"]), name
+        else:
+            assert sha(bits(aabbs)) == str(golden[name + "/sha_aabbs"]), name
+            assert sha(cells) == str(golden[name + "/sha_cells"]), name
+            assert sha(idx) == str(golden[name + "/sha_indices"]), name
+
+
+def test_golden_cases_through_the_stateless_entry_points(gpu, golden):
+    for name, v in golden_views(golden):
+        aabbs, cells, idx = run_stateless(v)
+        if name + "/aabbs" in golden.files:
+            assert np.array_equal(bits(aabbs), golden[name + "/aabbs"]), name
+            assert np.array_equal(cells, golden[name + "/cells"]), name
+            assert np.array_equal(idx, golden[name + "/indices"]), name
+
+
+def test_plain_small_full_size(gpu, oracle):
+    v = scenes.plain_small(1)
+    assert_matches_oracle(oracle, v, *run_pipeline(gpu, v))
+
+
+def test_plain_large_full_size(gpu, oracle):
+    v = scenes.plain_large(2)
+    assert_matches_oracle(oracle, v, *run_pipeline(gpu, v))
+
+
+@pytest.mark.parametrize("tuning", TUNINGS)
+def test_every_kernel_configuration(gpu, oracle, golden, tuning):
+    views = dict(golden_views(golden))
+    for name in ("cap_dense", "all_capped", "nonfinite_lights", "odd_grid_odd_lights", "grid_1x1x1"):
+        assert_matches_oracle(oracle, views[name], *run_pipeline(gpu, views[name], tuning))
+    v = scenes.plain_large(9, n_lights=3000)
+    assert_matches_oracle(oracle, v, *run_pipeline(gpu, v, tuning))
+
+
+def test_batch_mix_views(gpu, oracle):
+    views = scenes.batch_mix(3, n_views=12)
+    views.sort(key=lambda v: -v.light_count)
+    for v in views[:3] + views[-3:]:  # the largest (up to 65536 lights) and the smallest
+        assert_matches_oracle(oracle, v, *run_pipeline(gpu, v))
+
+
+def test_aabbs_over_varied_projections(gpu, oracle):
+    """Exercises the pinned pow and the mat4 order on the device."""
+    rng = np.random.default_rng(11)
+    for _ in range(12):
+        grid = (int(rng.integers(1, 40)), int(rng.integers(1, 30)), int(rng.integers(1, 64)))
+        near = float(rng.uniform(0.01, 2.0))
+        far = float(near * 10 ** rng.uniform(0.5, 5))
+        fovy = float(np.radians(rng.uniform(20, 110)))
+        v = scenes.custom_view(grid, int(rng.integers(64, 4096)), int(rng.integers(64, 4096)), near, far,
+                               view=look_at_rh(rng.uniform(-5, 5, 3), rng.uniform(-5, 5, 3) + [0, 0, -10]),
+                               lights=scenes.uniform_box_lights(rng, 100, [-50, -50, -200], [50, 50, 10]), fovy=fovy)
+        assert_matches_oracle(oracle, v, *run_stateless(v))
+
+
+def test_known_answer_cap_order(gpu, oracle):
+    v = scenes.custom_view((1, 1, 1), 100, 100, 1.0, 10.0)
+    a = oracle.generate_aabbs(v.ubo)
+    centre = (a[0, 0:3] + a[0, 4:7]) / 2
+    pos = np.array([[0.0, 0.0, 1e4] if i % 3 == 0 else centre for i in range(400)], np.float32)
+    v.lights = scenes.make_lights(pos, np.ones(400, np.float32))
+    aabbs, cells, idx = run_pipeline(gpu, v)
+    assert list(idx) == [i for i in range(400) if i % 3 != 0][:150]
+
+
+def test_deterministic_across_runs_and_streams(gpu):
+    import torch
+    v = scenes.plain_large(4, n_lights=8000)
+    a1 = run_pipeline(gpu, v)
+    s = torch.cuda.Stream()
+    a2 = run_pipeline(gpu, v, stream=s)
+    for x, y in zip(a1, a2):
+        assert np.array_equal(np.asarray(x).view(np.uint32), np.asarray(y).view(np.uint32))
+
+
+def test_pipeline_semantics(gpu, oracle):
+    """aabbDirty_ handling, UpdateLightPosition and ResetGlobalIndex."""
+    from hellovulkan_gb300.pipelines import (PipelineAABBGenerator, PipelineLightCulling, ResourcesClusterForward,
+                                             ResourcesLight)
+    v = scenes.plain_small(2)
+    rl = ResourcesLight(gpu)
+    rl.add_lights(v.lights)
+    assert rl.light_count == v.light_count and rl.device_buffer != 0
+    rc = ResourcesClusterForward(gpu)
+    rc.create_buffers(16, 9, 24, 150)
+    gen = PipelineAABBGenerator(gpu, rc)
+    cull = PipelineLightCulling(gpu, rl, rc)
+    assert rc.aabb_dirty
+    gen.set_cluster_forward_ubo(v.ubo)
+    gen.fill_command_buffer()
+    assert not rc.aabb_dirty
+    gen.set_cluster_forward_ubo(v.ubo)  # same projection: stays clean
+    assert not rc.aabb_dirty
+    gen.on_window_resized()
+    assert rc.aabb_dirty
+    gen.fill_command_buffer()
+    zoomed = scenes.custom_view((16, 9, 24), 1920, 1080, 0.1, 1000.0, fovy=np.radians(30.0)).ubo
+    gen.set_cluster_forward_ubo(zoomed)  # a zoom changes the projection: dirty again
+    assert rc.aabb_dirty
+    gen.set_cluster_forward_ubo(v.ubo)
+    gen.fill_command_buffer()
+    # move one light, as ResourcesLight::UpdateLightPosition
+    moved = v.lights.copy()
+    moved[7, :4] = [1.0, 2.0, -30.0, 1.0]
+    rl.update_light_position(7, (1.0, 2.0, -30.0))
+    rl.update_light_position(10 ** 6, (0.0, 0.0, 0.0))  # out of range: ignored
+    cull.reset_global_index()
+    cull.set_cluster_forward_ubo(v.ubo)
+    cull.fill_command_buffer()
+    cells, idx = rc.read_outputs()
+    a = oracle.generate_aabbs(v.ubo)
+    oc, oi, _ = oracle.cull(v.ubo, a, moved)
+    assert np.array_equal(cells, oc) and np.array_equal(idx, oi)
+    # running twice without re-uploading gives the same result (no counter to reset)
+    cull.fill_command_buffer()
+    cells2, idx2 = rc.read_outputs()
+    assert np.array_equal(cells, cells2) and np.array_equal(idx, idx2)
+
+
+def test_pipeline_error_paths(gpu):
+    from hellovulkan_gb300 import CfError
+    from hellovulkan_gb300.pipelines import (PipelineAABBGenerator, PipelineLightCulling, ResourcesClusterForward,
+                                             ResourcesLight)
+    rl, rc = ResourcesLight(gpu), ResourcesClusterForward(gpu)
+    gen, cull = PipelineAABBGenerator(gpu, rc), PipelineLightCulling(gpu, rl, rc)
+    with pytest.raises(CfError) as e:
+        gen.fill_command_buffer()
+    assert e.value.status == 5  # no UBO yet
+    with pytest.raises(CfError) as e:
+        rc.create_buffers(0, 9, 24)
+    assert e.value.status == 1
+    rc.create_buffers(16, 9, 24)
+    v = scenes.plain_small(1)
+    cull.set_cluster_forward_ubo(v.ubo)
+    with pytest.raises(CfError) as e:
+        cull.fill_command_buffer()  # the AABB generator never ran
+    assert e.value.status == 5
+    wrong = scenes.custom_view((8, 8, 8), 100, 100, 0.1, 10.0).ubo
+    gen.set_cluster_forward_ubo(wrong)
+    with pytest.raises(CfError) as e:
+        gen.fill_command_buffer()
+    assert e.value.status == 1

@@ -118,6 +118,7 @@ _SIGS = {
     "cf_generate_aabbs": [C.POINTER(CfClusterForwardUBO), _P, _P],
     "cf_cull_lights": [C.POINTER(CfClusterForwardUBO), _P, _P, _U32, _U32, _P, _P, _U64, _P, _P, _U64, _P],
     "cf_cull_workspace_device_error": [_P, _PU32],
+    "cf_cull_lights_static_scratch": [C.POINTER(CfClusterForwardUBO), _P, _P, _U32, _U32, _P, _P, _U64, _P, _P, _P],
 }
 _RESTYPE = {"cf_status_string": C.c_char_p, "cf_last_error_message": C.c_char_p}
 

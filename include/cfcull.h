@@ -210,6 +210,24 @@ CFCULL_API int cf_cull_lights(const CfClusterForwardUBO* ubo, const CfAABB* d_aa
  * (0 = none; CF_ERROR_DEVICE_TIMEOUT otherwise).  Synchronises the device. */
 CFCULL_API int cf_cull_workspace_device_error(void* d_workspace, uint32_t* device_error);
 
+/* No counterpart in the reference (its Vulkan buffers are all created up
+ * front).  cf_cull_lights for callers that cannot allocate device memory when
+ * they cull — a frame recorded inside a host allocator's critical section, a
+ * plugin whose device memory its host reserves, a real-time loop that cannot
+ * afford cudaMalloc/cudaFree.  Same inputs and outputs as cf_cull_lights, but
+ * the scratch comes from a fixed 32 MiB device array that every GPU loading
+ * this library holds until the process exits; views needing more scratch are
+ * rejected with CF_ERROR_CAPACITY.  The first call on a device looks up that
+ * array's address and should come before any stream capture.  All calls on a
+ * device share the array: calls that overlap on the GPU race and must be
+ * serialised.  d_device_error (optional, device) receives the bounded-wait
+ * error bits; without it they go to the array's own word, cleared per call. */
+CFCULL_API int cf_cull_lights_static_scratch(const CfClusterForwardUBO* ubo, const CfAABB* d_aabbs,
+                                             const CfLightData* d_lights, uint32_t light_count,
+                                             uint32_t max_lights_per_cluster, CfLightCell* d_cells,
+                                             uint32_t* d_indices, uint64_t index_capacity, uint32_t* d_total,
+                                             uint32_t* d_device_error, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

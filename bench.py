@@ -48,6 +48,8 @@ OPS_PER_TEST = 16
 L2_FLUSH_BYTES = 256 << 20
 SMS = 152
 FP32_LANES_PER_SM = 128
+PLAIN_SMALL = (1, 8, 512, 4, 0)  # brute-force culling configurations
+PLAIN_LARGE = (2, 8, 512, 4, 0)
 
 
 def parse():
@@ -57,7 +59,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--workload", choices=["plain_large", "plain_small"], default="plain_large")
-    p.add_argument("--tuning", type=str, default="", help="K,warps,tile,stages of the culling kernel")
+    p.add_argument("--tuning", type=str, default="", help="K,warps,tile,stages,binned of the culling kernel")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline budget")
     return p.parse_args()
@@ -250,6 +252,23 @@ def run_ours(args):
 
     cull.set_cluster_forward_ubo(view.ubo)
     cull.enable_stage_timing(True)
+
+    def timed_steps(n):
+        """n steps, L2 flushed before each, each bracketed by CUDA events on the
+        launching stream; returns (sum of step ms, per-step stage ms)."""
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+        stage = np.zeros((n, 3))
+        for i in range(n):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            starts[i].record(stream)
+            cull.fill_command_buffer(stream)
+            ends[i].record(stream)
+            stage[i] = cull.stage_times_ms()
+        torch.cuda.synchronize()
+        return float(sum(s.elapsed_time(e) for s, e in zip(starts, ends))), stage
+
     for _ in range(args.warmup):
         cull.fill_command_buffer(stream)
     stream.synchronize()
@@ -258,19 +277,7 @@ def run_ours(args):
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    stage = np.zeros((args.steps, 3))
-    for i in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        starts[i].record(stream)
-        cull.fill_command_buffer(stream)
-        ends[i].record(stream)
-        stage[i] = cull.stage_times_ms()
-    torch.cuda.synchronize()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = float(sum(step_ms))
+    total_ms, stage = timed_steps(args.steps)
 
     # e2e through the C ABI with host buffers
     b = rc.buffers()
@@ -298,7 +305,21 @@ def run_ours(args):
     e2e_s = time.perf_counter() - t0
     clocks = sampler.stop()
 
-    # correctness of what was timed (rank 0, last result) against the oracle
+    # untimed: the tests the kernels executed in one step (work counters), and
+    # the brute-force kernel on the same view (every light against every cluster)
+    cull.enable_work_counters(True)
+    cull.fill_command_buffer(stream)
+    work_filter, work_cluster = cull.read_work_counters()
+    cull.enable_work_counters(False)
+    cull.enable_stage_timing(True)
+    plain_steps = max(3, min(args.steps, 200))
+    cull.set_tuning(*(PLAIN_SMALL if view.clusters <= 8192 else PLAIN_LARGE))
+    for _ in range(3):
+        cull.fill_command_buffer(stream)
+    plain_ms, plain_stage = timed_steps(plain_steps)
+    cull.set_tuning(0)
+    cull.enable_stage_timing(False)
+
     tests_per_view = view.clusters * view.light_count
     stats = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device="cuda")
     if ws > 1:
@@ -308,6 +329,7 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
         return
 
+    # correctness of what was timed (rank 0, last e2e result) against the oracle
     from oracle import Oracle
     o = Oracle()
     o_aabbs = o.generate_aabbs(view.ubo)
@@ -316,24 +338,41 @@ def run_ours(args):
                   and total_indices == o_idx.size)
 
     value = ws * tests_per_view * args.steps / (total_ms * 1e-3)
-    cull_ms = float(np.mean(stage[:, 1]))
-    achieved = executed * OPS_PER_TEST / (cull_ms * 1e-3) / 1e12
     sm_max = clocks.get("sm_max_mhz") or 2070.0
-    peak = SMS * FP32_LANES_PER_SM * sm_max * 1e6 / 1e12
-    traffic = None
-    prof = REPO / "profiles" / "cull_dram_bytes.json"
-    if prof.exists():
-        try:
-            traffic = json.loads(prof.read_text()).get(args.workload)
-        except ValueError:
-            traffic = None
-    alg_bytes = 16 * view.light_count + 32 * view.clusters + 4 * view.clusters + 4 * o_idx.size
+    fp32_peak = SMS * FP32_LANES_PER_SM * sm_max * 1e6 / 1e12
+    peak_note = ("nominal FP32 issue rate, %d SMs x %d lanes x %.0f MHz (no measured FP32 peak exists in "
+                 "MEASURED_PEAKS.json)" % (SMS, FP32_LANES_PER_SM, sm_max))
     peaks = {}
     try:
         peaks = json.loads((REPO / "MEASURED_PEAKS.json").read_text())
     except (OSError, ValueError):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    traffic = {}
+    prof = REPO / "profiles" / "dram_bytes_per_launch.json"
+    if prof.exists():
+        try:
+            traffic = json.loads(prof.read_text()).get(args.workload, {})
+        except ValueError:
+            traffic = {}
+    st_x, st_c, st_f = (float(np.mean(stage[:, i])) for i in range(3))
+    H = o_idx.size
+    cull_ops = (work_filter + work_cluster) * OPS_PER_TEST
+    fin_bytes = 12 * view.clusters + 8 * H
+    if st_c >= st_f:
+        ach = cull_ops / (st_c * 1e-3) / 1e12
+        roof = {"bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "Tops/s", "frac": ach / fp32_peak,
+                "traffic": traffic.get("cull"), "kernel": "bin_slices_kernel + cull_kernel (binned)",
+                "ops_per_launch": cull_ops, "peak_source": peak_note,
+                "work": "executed sphere-box tests x %d ops (work counters): %d slab/union + %d cluster" % (
+                    OPS_PER_TEST, work_filter, work_cluster)}
+    else:
+        ach = fin_bytes / (st_f * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak,
+                "traffic": traffic.get("finalize"), "kernel": "finalize_kernel", "bytes_per_launch": fin_bytes,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
+    p_x, p_c, p_f = (float(np.mean(plain_stage[:, i])) for i in range(3))
+    p_ach = executed * OPS_PER_TEST / (p_c * 1e-3) / 1e12
     bi = view.light_count * 48
     bo = view.clusters * 8 + total_indices * 4 + 4
     cpu = None
@@ -345,28 +384,28 @@ def run_ours(args):
     cfg.update({"parallelism": "replicas x%d" % ws if ws > 1 else "single GPU",
                 "l2": "flushed between timed steps (256 MiB write)",
                 "aabbs": "generated once per projection (%.4f ms, not in the step)" % aabb_ms,
-                "step": "light transform + culling + offset scan"})
+                "step": "light transform + slice binning + culling + offset scan"})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded)", "config": cfg,
         "views_per_s": ws * args.steps / (total_ms * 1e-3),
         "parity_with_oracle": parity,
-        "stage_ms": {"light_transform": float(np.mean(stage[:, 0])), "cull": cull_ms,
-                     "offset_scan": float(np.mean(stage[:, 2]))},
-        "executed_tests_per_view": executed,
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "Tops/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "cull_kernel", "ops_per_launch": executed * OPS_PER_TEST,
-                     "peak_source": "nominal FP32 issue rate, %d SMs x %d lanes x %.0f MHz (no measured FP32 peak "
-                                    "exists in MEASURED_PEAKS.json)" % (SMS, FP32_LANES_PER_SM, sm_max)},
-        "roofline_hbm": {"achieved": alg_bytes / (cull_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": alg_bytes / (cull_ms * 1e-3) / 1e9 / hbm_peak, "bytes_per_launch": alg_bytes},
+        "stage_ms": {"light_transform": st_x, "bin_and_cull": st_c, "offset_scan": st_f},
+        "executed_tests_per_view_reference_loop": executed,
+        "executed_tests_per_view_kernels": work_filter + work_cluster,
+        "roofline": roof,
+        "plain_kernel": {"note": "brute force: every light against every cluster, same view",
+                         "ms_per_step": plain_ms / plain_steps, "value": tests_per_view * plain_steps / (plain_ms * 1e-3),
+                         "stage_ms": {"light_transform": p_x, "cull": p_c, "offset_scan": p_f},
+                         "roofline": {"bound": "fp32", "achieved": p_ach, "peak": fp32_peak, "unit": "Tops/s",
+                                      "frac": p_ach / fp32_peak, "kernel": "cull_kernel (brute force)",
+                                      "ops_per_launch": executed * OPS_PER_TEST, "traffic": traffic.get("cull_plain")}},
         "cpu_baseline": cpu,
         "e2e": {"value": ws * tests_per_view * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": bi,
                 "d2h_bytes_per_step": bo, "ms_per_step": 1e3 * e2e_s / e2e_steps, "steps": e2e_steps,
                 "timing": "host clock, synchronised, pinned host buffers"},
-        "gpu_launches": 3 * (args.steps + e2e_steps),
+        "gpu_launches": 4 * (args.steps + e2e_steps),
         "clocks": clocks,
     }
     print(json.dumps(line), flush=True)

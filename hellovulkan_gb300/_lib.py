@@ -111,10 +111,12 @@ _SIGS = {
     "cf_pipeline_light_culling_reset_global_index": [_P],
     "cf_pipeline_light_culling_set_cluster_forward_ubo": [_P, C.POINTER(CfClusterForwardUBO)],
     "cf_pipeline_light_culling_fill_command_buffer": [_P, _P],
-    "cf_pipeline_light_culling_set_tuning": [_P, _I, _I, _I, _I],
+    "cf_pipeline_light_culling_set_tuning": [_P, _I, _I, _I, _I, _I],
     "cf_pipeline_light_culling_enable_stage_timing": [_P, _I],
     "cf_pipeline_light_culling_get_stage_times": [_P, C.POINTER(C.c_float)],
-    "cf_cull_workspace_size": [_U32, _U32, _U32, _PU64],
+    "cf_pipeline_light_culling_enable_work_counters": [_P, _I],
+    "cf_pipeline_light_culling_read_work_counters": [_P, _PU64],
+    "cf_cull_workspace_size": [C.POINTER(CfClusterForwardUBO), _U32, _U32, _PU64],
     "cf_generate_aabbs": [C.POINTER(CfClusterForwardUBO), _P, _P],
     "cf_cull_lights": [C.POINTER(CfClusterForwardUBO), _P, _P, _U32, _U32, _P, _P, _U64, _P, _P, _U64, _P],
     "cf_cull_workspace_device_error": [_P, _PU32],

@@ -98,6 +98,14 @@ __device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void* src, uin
         : "memory");
 }
 
+// Named barrier 1 over the first N threads of the CTA (the consumer warps;
+// the producer warp never takes part).
+template <int N>
+__device__ __forceinline__ void consumer_sync()
+{
+    asm volatile("bar.sync 1, %0;" ::"n"(N) : "memory");
+}
+
 __device__ __forceinline__ float max3f(float a, float b, float c)
 {
     float r;
@@ -108,6 +116,23 @@ __device__ __forceinline__ float max3f(float a, float b, float c)
 __device__ __forceinline__ bool finite_bits(float x)
 {
     return (__float_as_uint(x) & 0x7f800000u) != 0x7f800000u;
+}
+
+__device__ __forceinline__ uint32_t warp_sum(uint32_t x)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
+    return x;
+}
+
+__device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t x, uint32_t lane)
+{
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    return x;
 }
 
 // ---------------------------------------------------------------------------
@@ -243,18 +268,32 @@ struct WarpClusters {
     float mn[K][3];
     float mx[K][3];
     uint32_t cnt[K];
+    float umn[3], umx[3];  // union of the warp's valid boxes (NaN bounds widen it to +-inf)
 };
 
 // Tests the lights of one shared-memory tile against the warp's K clusters;
 // returns true once every cluster of the warp has reached the cap.
-template <int K, bool kExact>
-__device__ __forceinline__ bool scan_tile(const float4* __restrict__ tile, uint32_t n, uint32_t base, uint32_t lane,
-                                          WarpClusters<K>& w, uint32_t cap, uint32_t* __restrict__ staging,
-                                          uint32_t cl0, uint32_t clusters)
+//   kExact   the shader's branchy test (tiles holding non-finite coordinates)
+//   kBinned  light indices come from idx_tile (a slice candidate list) instead
+//            of base + position, and each 32-light chunk is first tested
+//            against the warp's union box: a chunk no lane of which can reach
+//            the union cannot hit any of the K boxes (per axis the distance
+//            to a box that contains another is never larger, and the rounded
+//            sums are monotonic), so the K tests are skipped
+template <int K, bool kExact, bool kBinned>
+__device__ __forceinline__ bool scan_tile(const float4* __restrict__ tile, const uint32_t* __restrict__ idx_tile,
+                                          uint32_t n, uint32_t base, uint32_t lane, WarpClusters<K>& w, uint32_t cap,
+                                          uint32_t* __restrict__ staging, uint32_t cl0, uint32_t cl_end,
+                                          uint32_t& chunks_filtered, uint32_t& chunks_tested)
 {
     const uint32_t lt_mask = (1u << lane) - 1u;
     for (uint32_t j = 0; j < n; j += 32) {
         const float4 L = tile[j + lane];
+        if (kBinned) {
+            ++chunks_filtered;
+            if (!__any_sync(kFull, hit_fast(L, w.umn, w.umx))) continue;
+        }
+        ++chunks_tested;
         bool h[K];
         bool any = false;
 #pragma unroll
@@ -263,7 +302,7 @@ __device__ __forceinline__ bool scan_tile(const float4* __restrict__ tile, uint3
             any |= h[k];
         }
         if (__any_sync(kFull, any)) {
-            const uint32_t li = base + j + lane;
+            const uint32_t li = kBinned ? idx_tile[j + lane] : base + j + lane;
             bool all_capped = true;
 #pragma unroll
             for (int k = 0; k < K; ++k) {
@@ -282,7 +321,7 @@ __device__ __forceinline__ bool scan_tile(const float4* __restrict__ tile, uint3
                         }
                     }
                 }
-                all_capped = all_capped && (w.cnt[k] >= cap || cl0 + k >= clusters);
+                all_capped = all_capped && (w.cnt[k] >= cap || cl0 + k >= cl_end);
             }
             if (all_capped) return true;
         }
@@ -298,21 +337,48 @@ __device__ __forceinline__ bool tile_has_nonfinite(const uint32_t* __restrict__ 
 }
 
 // blockDim = (WARPS + 1) * 32: warps 0..WARPS-1 consume, warp WARPS produces.
-// Dynamic shared memory: STAGES x TILE float4, then the full/empty mbarriers,
-// the per-stage stop flags and the done-warp counter.
-template <int K, int WARPS, int TILE, int STAGES>
+// Dynamic shared memory: STAGES x TILE float4 (and, binned, STAGES x TILE
+// light indices), then the full/empty mbarriers, the per-stage stop flags and
+// the done-warp counter.
+//   plain   CTA b owns clusters [b*W*K, (b+1)*W*K) and streams every light
+//   binned  CTA b owns group g of slice k (b = k * groups_per_slice + g) and
+//           streams that slice's candidate list made by bin_slices_kernel
+template <int K, int WARPS, int TILE, int STAGES, bool kBinned>
 __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v, uint32_t* __restrict__ dev_error)
 {
     static_assert(TILE % 32 == 0, "tiles hold whole warps of lights");
     extern __shared__ __align__(128) unsigned char smem[];
     float4* tiles = reinterpret_cast<float4*>(smem);
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)STAGES * TILE * sizeof(float4));
+    uint32_t* idx_tiles = reinterpret_cast<uint32_t*>(smem + (size_t)STAGES * TILE * sizeof(float4));
+    unsigned char* tail = smem + (size_t)STAGES * TILE * (sizeof(float4) + (kBinned ? sizeof(uint32_t) : 0));
+    uint64_t* full = reinterpret_cast<uint64_t*>(tail);
     uint64_t* empty = full + STAGES;
     volatile uint32_t* stop = reinterpret_cast<volatile uint32_t*>(empty + STAGES);
     uint32_t* done_warps = reinterpret_cast<uint32_t*>(empty + STAGES) + STAGES;
+    // binned only: survivor buffer, per-chunk counts, per-warp union boxes, abort flag
+    unsigned char* binned_extra =
+        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(done_warps + 1) + 15) & ~uintptr_t(15));
+    (void)binned_extra;
 
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t ntiles = (v.lpad + TILE - 1) / TILE;
+    const float4* src = v.vlights;
+    const uint32_t* src_idx = nullptr;
+    uint32_t nsrc = v.lpad, first, cl_end;
+    bool slice_exact = false;
+    if (kBinned) {
+        const uint32_t xy = v.slice_clusters, gps = (xy + WARPS * K - 1) / (WARPS * K);
+        const uint32_t k = blockIdx.x / gps, g = blockIdx.x % gps;
+        src = v.slice_lights + (size_t)k * v.lpad;
+        src_idx = v.slice_idx + (size_t)k * v.lpad;
+        nsrc = v.slice_count[k];
+        slice_exact = v.slice_nonfinite[k] != 0;
+        first = k * xy + g * (uint32_t)(WARPS * K);
+        cl_end = (k + 1) * xy;
+    } else {
+        first = blockIdx.x * (uint32_t)(WARPS * K);
+        cl_end = v.clusters;
+    }
+    const uint32_t ntiles = (nsrc + TILE - 1) / TILE;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -340,181 +406,439 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
                     break;
                 }
                 stop[s] = 0;
-                const uint32_t n = min((uint32_t)TILE, v.lpad - t * TILE);
-                mbar_arrive_expect_tx(smem_u32(&full[s]), n * (uint32_t)sizeof(float4));
-                bulk_copy_g2s(smem_u32(tiles + (size_t)s * TILE), v.vlights + (size_t)t * TILE,
+                const uint32_t n = min((uint32_t)TILE, nsrc - t * TILE);
+                const uint32_t bytes = n * (uint32_t)(sizeof(float4) + (kBinned ? sizeof(uint32_t) : 0));
+                mbar_arrive_expect_tx(smem_u32(&full[s]), bytes);
+                bulk_copy_g2s(smem_u32(tiles + (size_t)s * TILE), src + (size_t)t * TILE,
                               n * (uint32_t)sizeof(float4), smem_u32(&full[s]));
+                if (kBinned)
+                    bulk_copy_g2s(smem_u32(idx_tiles + (size_t)s * TILE), src_idx + (size_t)t * TILE,
+                                  n * (uint32_t)sizeof(uint32_t), smem_u32(&full[s]));
             }
         }
         return;
     }
 
     // Consumers.
-    const uint32_t cl0 = blockIdx.x * (uint32_t)(WARPS * K) + warp * (uint32_t)K;
+    const uint32_t cl0 = first + warp * (uint32_t)K;
+    const float inf = __uint_as_float(0x7f800000u);
     WarpClusters<K> w;
-    bool done = true;
+    bool done = true, union_nan = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        w.umn[a] = inf;
+        w.umx[a] = -inf;
+    }
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         w.cnt[k] = 0;
         const uint32_t c = cl0 + k;
-        if (c < v.clusters) {
+        if (c < cl_end) {
             const float4 a = v.aabbs[2 * (size_t)c];
             const float4 b = v.aabbs[2 * (size_t)c + 1];
             w.mn[k][0] = a.x; w.mn[k][1] = a.y; w.mn[k][2] = a.z;
             w.mx[k][0] = b.x; w.mx[k][1] = b.y; w.mx[k][2] = b.z;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                union_nan |= (w.mn[k][q] != w.mn[k][q]) | (w.mx[k][q] != w.mx[k][q]);
+                w.umn[q] = fminf(w.umn[q], w.mn[k][q]);
+                w.umx[q] = fmaxf(w.umx[q], w.mx[k][q]);
+            }
             done = false;
         } else {
-            const float inf = __uint_as_float(0x7f800000u);
-            for (int a = 0; a < 3; ++a) { w.mn[k][a] = inf; w.mx[k][a] = inf; }
+            for (int q = 0; q < 3; ++q) { w.mn[k][q] = inf; w.mx[k][q] = inf; }
+        }
+    }
+    if (union_nan) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            w.umn[a] = -inf;
+            w.umx[a] = inf;
         }
     }
     if (done && lane == 0) atomicAdd(done_warps, 1u);
 
-    for (uint32_t t = 0; t < ntiles; ++t) {
-        const uint32_t s = t % STAGES;
-        if (!mbar_wait_bounded(smem_u32(&full[s]), (t / STAGES) & 1u)) {
-            if (lane == 0) atomicOr(dev_error, kErrFullWaitTimeout);
-            break;
+    uint32_t chunks_filtered = 0, chunks_tested = 0;
+    if constexpr (kBinned) {
+        // The CTA's consumer warps share the filtering of each tile: warp w
+        // tests chunks w, w + WARPS, ... against the union box of all the
+        // CTA's clusters, the survivors are compacted in light order into
+        // shared memory (ballot/popc and a prefix over the tile's chunks),
+        // and every warp then tests only the survivors against its K boxes.
+        constexpr uint32_t kChunks = TILE / 32;
+        constexpr int kPer = (int)((kChunks + WARPS - 1) / WARPS);
+        float4* surv_l = reinterpret_cast<float4*>(binned_extra);
+        uint32_t* surv_i = reinterpret_cast<uint32_t*>(surv_l + TILE);
+        uint32_t* s_cnt = surv_i + TILE;
+        float* s_box = reinterpret_cast<float*>(s_cnt + kChunks);
+        volatile uint32_t* s_abort = reinterpret_cast<volatile uint32_t*>(s_box + WARPS * 8);
+        if (lane == 0) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                s_box[warp * 8 + a] = w.umn[a];
+                s_box[warp * 8 + 3 + a] = w.umx[a];
+            }
+            if (warp == 0) *s_abort = 0;
         }
-        if (stop[s]) break;
-        if (!done) {
-            const uint32_t base = t * TILE;
-            const uint32_t n = min((uint32_t)TILE, v.lpad - base);
+        consumer_sync<WARPS * 32>();
+        float cmn[3] = {inf, inf, inf}, cmx[3] = {-inf, -inf, -inf};
+        for (int q = 0; q < WARPS; ++q) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                cmn[a] = fminf(cmn[a], s_box[q * 8 + a]);
+                cmx[a] = fmaxf(cmx[a], s_box[q * 8 + 3 + a]);
+            }
+        }
+        const uint32_t lt_mask = (1u << lane) - 1u;
+        for (uint32_t t = 0; t < ntiles; ++t) {
+            const uint32_t s = t % STAGES;
+            if (!mbar_wait_bounded(smem_u32(&full[s]), (t / STAGES) & 1u) && lane == 0) {
+                atomicOr(dev_error, kErrFullWaitTimeout);
+                *s_abort = 1;
+            }
+            consumer_sync<WARPS * 32>();  // every warp leaves together on a timeout
+            if (*s_abort || stop[s]) break;
+            const uint32_t n = min((uint32_t)TILE, nsrc - t * TILE);
             const float4* tile = tiles + (size_t)s * TILE;
-            if (!tile_has_nonfinite(v.nonfinite, base, n))
-                done = scan_tile<K, false>(tile, n, base, lane, w, v.cap, v.staging, cl0, v.clusters);
-            else
-                done = scan_tile<K, true>(tile, n, base, lane, w, v.cap, v.staging, cl0, v.clusters);
-            if (done && lane == 0) atomicAdd(done_warps, 1u);
+            const uint32_t* itile = idx_tiles + (size_t)s * TILE;
+            float4 Ls[kPer];
+            uint32_t Is[kPer], Ms[kPer];
+#pragma unroll
+            for (int q = 0; q < kPer; ++q) {
+                const uint32_t ch = warp + q * WARPS;
+                bool pass = false;
+                if (ch < kChunks && ch * 32 < n) {
+                    Ls[q] = tile[ch * 32 + lane];
+                    Is[q] = itile[ch * 32 + lane];
+                    pass = hit_fast(Ls[q], cmn, cmx);
+                    ++chunks_filtered;
+                }
+                Ms[q] = __ballot_sync(kFull, pass);
+                if (ch < kChunks && lane == 0) s_cnt[ch] = __popc(Ms[q]);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&empty[s]));  // the stage is no longer read
+            consumer_sync<WARPS * 32>();
+            const uint32_t cnt = lane < kChunks ? s_cnt[lane] : 0u;
+            const uint32_t incl = warp_inclusive_scan(cnt, lane);
+            const uint32_t ns = __shfl_sync(kFull, incl, 31);
+#pragma unroll
+            for (int q = 0; q < kPer; ++q) {
+                const uint32_t ch = warp + q * WARPS;
+                const uint32_t excl = __shfl_sync(kFull, incl - cnt, ch & 31);
+                if (ch < kChunks && ((Ms[q] >> lane) & 1u)) {
+                    const uint32_t p = excl + __popc(Ms[q] & lt_mask);
+                    surv_l[p] = Ls[q];
+                    surv_i[p] = Is[q];
+                }
+            }
+            const uint32_t nsp = (ns + 31) & ~31u;
+            if (warp == 0 && ns + lane < nsp) surv_l[ns + lane] = make_float4(0.f, 0.f, 0.f, -inf);
+            consumer_sync<WARPS * 32>();
+            if (!done && ns) {
+                done = slice_exact ? scan_tile<K, true, true>(surv_l, surv_i, nsp, 0, lane, w, v.cap, v.staging, cl0,
+                                                              cl_end, chunks_filtered, chunks_tested)
+                                   : scan_tile<K, false, true>(surv_l, surv_i, nsp, 0, lane, w, v.cap, v.staging, cl0,
+                                                               cl_end, chunks_filtered, chunks_tested);
+                if (done && lane == 0) atomicAdd(done_warps, 1u);
+            }
+            consumer_sync<WARPS * 32>();  // the survivor buffer is rewritten by the next tile
         }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(smem_u32(&empty[s]));
+    } else {
+        for (uint32_t t = 0; t < ntiles; ++t) {
+            const uint32_t s = t % STAGES;
+            if (!mbar_wait_bounded(smem_u32(&full[s]), (t / STAGES) & 1u)) {
+                if (lane == 0) atomicOr(dev_error, kErrFullWaitTimeout);
+                break;
+            }
+            if (stop[s]) break;
+            if (!done) {
+                const uint32_t base = t * TILE;
+                const uint32_t n = min((uint32_t)TILE, nsrc - base);
+                const float4* tile = tiles + (size_t)s * TILE;
+                if (!tile_has_nonfinite(v.nonfinite, base, n))
+                    done = scan_tile<K, false, false>(tile, nullptr, n, base, lane, w, v.cap, v.staging, cl0, cl_end,
+                                                      chunks_filtered, chunks_tested);
+                else
+                    done = scan_tile<K, true, false>(tile, nullptr, n, base, lane, w, v.cap, v.staging, cl0, cl_end,
+                                                     chunks_filtered, chunks_tested);
+                if (done && lane == 0) atomicAdd(done_warps, 1u);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&empty[s]));
+        }
     }
 
+    __shared__ uint32_t s_gsum[WARPS];
     if (lane == 0) {
+        uint32_t sum = 0;
 #pragma unroll
         for (int k = 0; k < K; ++k)
-            if (cl0 + k < v.clusters) v.counts[cl0 + k] = w.cnt[k];
+            if (cl0 + k < cl_end) {
+                v.counts[cl0 + k] = w.cnt[k];
+                sum += w.cnt[k];
+            }
+        s_gsum[warp] = sum;
+        if (v.work) {
+            atomicAdd(&v.work[0], 32ull * chunks_filtered);
+            atomicAdd(&v.work[1], 32ull * K * chunks_tested);
+        }
+    }
+    consumer_sync<WARPS * 32>();
+    if (threadIdx.x == 0) {  // this CTA's group is group blockIdx.x
+        uint32_t sum = 0;
+        for (int q = 0; q < WARPS; ++q) sum += s_gsum[q];
+        v.group_sums[blockIdx.x] = sum;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Slice binning: for depth slice k, the lights whose sphere can reach the
+// slab between the slice's lowest AABB min.z and highest AABB max.z, in
+// ascending light order, padded with never-hit entries to a multiple of 32.
+// A light left out fails every cluster of the slice: its z distance to the
+// slab is never larger than to a cluster's box, and the shader's sum of
+// squares is never smaller than its z term.  NaN bounds make the slab
+// infinite; a NaN coordinate contributes 0 and is kept; slices holding a
+// light with a non-finite coordinate are flagged for the exact test.
+// One 256-thread CTA per slice; each iteration bins 1024 lights (4 chunks of
+// 32 per warp) with ballot/popc and a block prefix over the 8 warps.
+// ---------------------------------------------------------------------------
+constexpr int kBinWarps = 32;
+constexpr int kBinChunks = 4;
+
+__global__ void __launch_bounds__(kBinWarps * 32) bin_slices_kernel(const ViewCull v)
+{
+    __shared__ float s_lo[kBinWarps], s_hi[kBinWarps];
+    __shared__ uint32_t s_cnt[kBinWarps];
+    __shared__ int s_nan, s_nonfinite;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t k = blockIdx.x, xy = v.slice_clusters;
+    const float inf = __uint_as_float(0x7f800000u);
+
+    float lo = inf, hi = -inf;
+    bool nan = false;
+    for (uint32_t c = tid; c < xy; c += kBinWarps * 32) {
+        const float a = v.aabbs[2 * ((size_t)k * xy + c)].z;
+        const float b = v.aabbs[2 * ((size_t)k * xy + c) + 1].z;
+        nan |= (a != a) | (b != b);
+        lo = fminf(lo, a);
+        hi = fmaxf(hi, b);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(kFull, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(kFull, hi, o));
+    }
+    if (tid == 0) s_nonfinite = 0;
+    if (lane == 0) {
+        s_lo[warp] = lo;
+        s_hi[warp] = hi;
+    }
+    const int any_nan = __syncthreads_or(nan);
+    lo = s_lo[0];
+    hi = s_hi[0];
+    for (int q = 1; q < kBinWarps; ++q) {
+        lo = fminf(lo, s_lo[q]);
+        hi = fmaxf(hi, s_hi[q]);
+    }
+    if (any_nan) {
+        lo = -inf;
+        hi = inf;
+    }
+
+    float4* out_l = v.slice_lights + (size_t)k * v.lpad;
+    uint32_t* out_i = v.slice_idx + (size_t)k * v.lpad;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    uint32_t running = 0;
+    bool nonfinite = false;
+    constexpr uint32_t kStep = kBinWarps * kBinChunks * 32;
+    for (uint32_t base = 0; base < v.lpad; base += kStep) {
+        float4 L[kBinChunks];
+        uint32_t m[kBinChunks];
+        uint32_t wcount = 0;
+#pragma unroll
+        for (int q = 0; q < kBinChunks; ++q) {
+            const uint32_t i = base + warp * (kBinChunks * 32) + q * 32 + lane;
+            L[q] = i < v.lpad ? v.vlights[i] : make_float4(0.f, 0.f, 0.f, -inf);
+            const float dz = max3f(__fsub_rn(lo, L[q].z), __fsub_rn(L[q].z, hi), 0.0f);
+            const bool pass = __fmul_rn(dz, dz) < L[q].w;
+            nonfinite |= pass && !(finite_bits(L[q].x) && finite_bits(L[q].y) && finite_bits(L[q].z));
+            m[q] = __ballot_sync(kFull, pass);
+            wcount += __popc(m[q]);
+        }
+        if (lane == 0) s_cnt[warp] = wcount;
+        __syncthreads();
+        uint32_t pos = running, total = 0;
+#pragma unroll
+        for (int q = 0; q < kBinWarps; ++q) {
+            const uint32_t cq = s_cnt[q];
+            pos += (q < (int)warp) ? cq : 0u;
+            total += cq;
+        }
+#pragma unroll
+        for (int q = 0; q < kBinChunks; ++q) {
+            if ((m[q] >> lane) & 1u) {
+                const uint32_t p = pos + __popc(m[q] & lt_mask);
+                out_l[p] = L[q];
+                out_i[p] = base + warp * (kBinChunks * 32) + q * 32 + lane;
+            }
+            pos += __popc(m[q]);
+        }
+        running += total;
+        __syncthreads();  // s_cnt is rewritten next iteration
+    }
+    if (nonfinite) s_nonfinite = 1;
+    const uint32_t npad = (running + 31) & ~31u;
+    for (uint32_t p = running + tid; p < npad; p += kBinWarps * 32) {
+        out_l[p] = make_float4(0.f, 0.f, 0.f, -inf);
+        out_i[p] = 0;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        v.slice_count[k] = npad;
+        v.slice_nonfinite[k] = s_nonfinite ? 1u : 0u;
+        if (v.work) atomicAdd(&v.work[0], (unsigned long long)v.lpad);
     }
 }
 
 // ---------------------------------------------------------------------------
 // Finalize: cells = exclusive scan of counts in cluster order, packed copy.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t warp_sum(uint32_t x)
+
+// Offset scan, one 1024-thread CTA per view: warp w owns the clusters
+// [w*rows*32, (w+1)*rows*32) as `rows` coalesced rows of 32; pass 1 sums
+// them, warp 0 scans the 32 warp sums, pass 2 scans each row with shuffles
+// and writes the LightCells.  O(C) work and no dependency between CTAs.
+constexpr uint32_t kScanThreads = 1024;
+__global__ void __launch_bounds__(kScanThreads) scan_kernel(const ViewCull v)
 {
+    constexpr uint32_t NW = kScanThreads / 32;
+    constexpr int R = 8;  // rows of 32 groups each warp holds in registers per pass
+    __shared__ uint32_t s_warp[NW];
+    __shared__ uint32_t s_total;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t C = v.groups;
+    uint32_t carry = 0;
+    for (uint32_t p0 = 0; p0 < C; p0 += kScanThreads * R) {
+        uint32_t n[R], inc[R], wsum = 0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
-    return x;
-}
-
-__device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t x, uint32_t lane)
-{
+        for (int r = 0; r < R; ++r) {  // all loads issued before any is used
+            const uint32_t c = p0 + (warp * R + r) * 32 + lane;
+            n[r] = c < C ? v.group_sums[c] : 0u;
+        }
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(kFull, x, o);
-        if (lane >= (uint32_t)o) x += y;
+        for (int r = 0; r < R; ++r) {
+            inc[r] = warp_inclusive_scan(n[r], lane);
+            wsum += __shfl_sync(kFull, inc[r], 31);
+        }
+        if (lane == 0) s_warp[warp] = wsum;
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t x = s_warp[lane];
+            const uint32_t i = warp_inclusive_scan(x, lane);
+            s_warp[lane] = i - x;
+            if (lane == 31) s_total = i;
+        }
+        __syncthreads();
+        uint32_t base = carry + s_warp[warp];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const uint32_t c = p0 + (warp * R + r) * 32 + lane;
+            if (c < C) v.group_offsets[c] = base + inc[r] - n[r];
+            base += __shfl_sync(kFull, inc[r], 31);
+        }
+        carry += s_total;
+        __syncthreads();  // s_warp / s_total are rewritten by the next pass
     }
-    return x;
+    if (v.total && threadIdx.x == 0) *v.total = carry;
 }
 
-__global__ void __launch_bounds__(1024) finalize_kernel(const ViewCull v)
+// LightCell and packed copy, one warp per cluster: its offset is its group's
+// offset plus the counts of the group's earlier clusters (one coalesced load
+// and a warp sum), then its staging slice is copied (at most cap / 32
+// coalesced iterations).  Every warp's loads are independent of the others'.
+constexpr uint32_t kCopyWarps = 8;
+__global__ void __launch_bounds__(kCopyWarps * 32) copy_kernel(const ViewCull v)
 {
-    static_assert(kFinalizeChunk == 2 * 1024, "two clusters per thread");
-    __shared__ uint32_t s_off[kFinalizeChunk];
-    __shared__ uint32_t s_warp[32];
-    __shared__ uint32_t s_base;
-    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t c0 = blockIdx.x * kFinalizeChunk;
-    const uint32_t C = v.clusters;
-
-    // Sum of the counts of every cluster before this chunk.
-    uint32_t acc = 0;
-    for (uint32_t i = tid; i < c0; i += 1024) acc += v.counts[i];
-    acc = warp_sum(acc);
-    if (lane == 0) s_warp[warp] = acc;
-    __syncthreads();
-    if (warp == 0) {
-        const uint32_t x = warp_sum(s_warp[lane]);
-        if (lane == 0) s_base = x;
+    const uint32_t c = blockIdx.x * kCopyWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (c >= v.clusters) return;
+    uint32_t b, first;
+    if (v.binned) {
+        const uint32_t gps = (v.slice_clusters + v.group_width - 1) / v.group_width;
+        const uint32_t k = c / v.slice_clusters, gi = (c % v.slice_clusters) / v.group_width;
+        b = k * gps + gi;
+        first = k * v.slice_clusters + gi * v.group_width;
+    } else {
+        b = c / v.group_width;
+        first = b * v.group_width;
     }
-    __syncthreads();
-    const uint32_t base = s_base;
-
-    // Exclusive scan of this chunk, two clusters per thread.
-    const uint32_t ca = c0 + 2 * tid, cb = ca + 1;
-    const uint32_t na = ca < C ? v.counts[ca] : 0u;
-    const uint32_t nb = cb < C ? v.counts[cb] : 0u;
-    const uint32_t mine = na + nb;
-    const uint32_t incl = warp_inclusive_scan(mine, lane);
-    if (lane == 31) s_warp[warp] = incl;
-    __syncthreads();
-    if (warp == 0) s_warp[lane] = warp_inclusive_scan(s_warp[lane], lane);
-    __syncthreads();
-    const uint32_t off_a = base + (warp ? s_warp[warp - 1] : 0u) + (incl - mine);
-    const uint32_t off_b = off_a + na;
-    if (ca < C) v.cells[ca] = CfLightCell{off_a, na};
-    if (cb < C) v.cells[cb] = CfLightCell{off_b, nb};
-    s_off[2 * tid] = off_a;
-    s_off[2 * tid + 1] = off_b;
-    if (v.total && blockIdx.x == gridDim.x - 1 && tid == 0) *v.total = base + s_warp[31];
-    __syncthreads();
-
-    // Packed copy: warp w moves clusters [w*64, w*64+64) of the chunk.
-    for (uint32_t q = 0; q < kFinalizeChunk / 32; ++q) {
-        const uint32_t local = warp * (kFinalizeChunk / 32) + q;
-        const uint32_t c = c0 + local;
-        if (c >= C) break;
-        const uint32_t n = v.counts[c];
-        const uint32_t o = s_off[local];
-        const uint32_t* src = v.staging + (size_t)c * v.cap;
-        for (uint32_t i = lane; i < n; i += 32) v.indices[o + i] = src[i];
-    }
+    const uint32_t cj = first + lane;
+    const uint32_t before = warp_sum(cj < c ? v.counts[cj] : 0u);
+    const uint32_t n = v.counts[c];
+    const uint32_t offset = v.group_offsets[b] + before;
+    if (lane == 0) v.cells[c] = CfLightCell{offset, n};
+    const uint32_t* src = v.staging + (size_t)c * v.cap;
+    for (uint32_t i = lane; i < n; i += 32) v.indices[offset + i] = src[i];
 }
 
-template <int K, int WARPS, int TILE, int STAGES>
+template <int K, int WARPS, int TILE, int STAGES, bool kBinned>
 cudaError_t launch_cull_t(const ViewCull& v, uint32_t* dev_error, cudaStream_t stream)
 {
-    const size_t smem = (size_t)STAGES * TILE * sizeof(float4) + 2 * STAGES * sizeof(uint64_t) +
-                        (STAGES + 1) * sizeof(uint32_t);
+    const size_t extra = kBinned ? 16 + (size_t)TILE * (sizeof(float4) + sizeof(uint32_t)) + (TILE / 32) * 4 +
+                                       (size_t)WARPS * 8 * sizeof(float) + sizeof(uint32_t)
+                                 : 0;
+    const size_t smem = (size_t)STAGES * TILE * (sizeof(float4) + (kBinned ? sizeof(uint32_t) : 0)) +
+                        2 * STAGES * sizeof(uint64_t) + (STAGES + 1) * sizeof(uint32_t) + extra;
     if (smem > 48 * 1024) {  // opt in above the default 48 KB (a per-device attribute)
-        const cudaError_t e = cudaFuncSetAttribute(cull_kernel<K, WARPS, TILE, STAGES>,
+        const cudaError_t e = cudaFuncSetAttribute(cull_kernel<K, WARPS, TILE, STAGES, kBinned>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
+    static_assert(WARPS * K <= 32, "a cluster group fits one warp of the copy kernel");
     const uint32_t per_cta = (uint32_t)(WARPS * K);
-    const uint32_t grid = (v.clusters + per_cta - 1) / per_cta;
-    cull_kernel<K, WARPS, TILE, STAGES><<<grid, (WARPS + 1) * 32, smem, stream>>>(v, dev_error);
+    const uint32_t grid = kBinned ? v.slices * ((v.slice_clusters + per_cta - 1) / per_cta)
+                                  : (v.clusters + per_cta - 1) / per_cta;
+    cull_kernel<K, WARPS, TILE, STAGES, kBinned><<<grid, (WARPS + 1) * 32, smem, stream>>>(v, dev_error);
     return cudaGetLastError();
 }
 
 }  // namespace
 
-#define CF_CULL_CONFIGS(X) \
-    X(1, 4, 512, 4)        \
-    X(2, 4, 512, 4)        \
-    X(4, 4, 512, 4)        \
-    X(1, 8, 512, 4)        \
-    X(2, 8, 512, 4)        \
-    X(4, 8, 512, 4)
+// (clusters per warp, consumer warps, lights per stage, stages, binned)
+#define CF_CULL_CONFIGS(X)  \
+    X(1, 4, 512, 4, false)  \
+    X(2, 4, 512, 4, false)  \
+    X(4, 4, 512, 4, false)  \
+    X(1, 8, 512, 4, false)  \
+    X(2, 8, 512, 4, false)  \
+    X(4, 8, 512, 4, false)  \
+    X(1, 4, 256, 4, true)   \
+    X(2, 4, 256, 4, true)   \
+    X(4, 4, 256, 4, true)   \
+    X(1, 8, 256, 4, true)   \
+    X(2, 8, 256, 4, true)   \
+    X(4, 8, 256, 4, true)
 
 bool cull_config_supported(const CullConfig& c)
 {
-#define CF_MATCH(K, W, T, S) \
-    if (c.clusters_per_warp == K && c.warps == W && c.tile == T && c.stages == S) return true;
+#define CF_MATCH(K, W, T, S, B) \
+    if (c.clusters_per_warp == K && c.warps == W && c.tile == T && c.stages == S && (c.binned != 0) == B) return true;
     CF_CULL_CONFIGS(CF_MATCH)
 #undef CF_MATCH
     return false;
 }
 
-CullConfig default_cull_config(uint32_t clusters, uint32_t lights)
+CullConfig default_cull_config(uint32_t clusters, uint32_t lights, uint32_t slices)
 {
     (void)lights;
-    if (clusters <= 8192) return CullConfig{1, 8, 512, 4};
-    return CullConfig{2, 8, 512, 4};
+    if (slices >= 2) return CullConfig{2, 8, 256, 4, 1};
+    if (clusters <= 8192) return CullConfig{1, 8, 512, 4, 0};
+    return CullConfig{2, 8, 512, 4, 0};
 }
 
-WorkspaceLayout workspace_layout(uint32_t clusters, uint32_t lights, uint32_t cap)
+WorkspaceLayout workspace_layout(uint32_t clusters, uint32_t lights, uint32_t cap, uint32_t slices, bool binned,
+                                 uint32_t groups)
 {
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     WorkspaceLayout w{};
@@ -528,6 +852,20 @@ WorkspaceLayout workspace_layout(uint32_t clusters, uint32_t lights, uint32_t ca
     off += al((size_t)clusters * sizeof(uint32_t));
     w.staging = off;
     off += al((size_t)clusters * cap * sizeof(uint32_t));
+    w.group_sums = off;
+    off += al((size_t)groups * sizeof(uint32_t));
+    w.group_offsets = off;
+    off += al((size_t)groups * sizeof(uint32_t));
+    if (binned) {
+        w.slice_lights = off;
+        off += al((size_t)slices * lpad * sizeof(float4));
+        w.slice_idx = off;
+        off += al((size_t)slices * lpad * sizeof(uint32_t));
+        w.slice_count = off;
+        off += al((size_t)slices * sizeof(uint32_t));
+        w.slice_nonfinite = off;
+        off += al((size_t)slices * sizeof(uint32_t));
+    }
     w.bytes = off;
     return w;
 }
@@ -551,12 +889,19 @@ cudaError_t launch_light_xform(const CfLightData* lights, uint32_t count, const 
     return cudaGetLastError();
 }
 
+cudaError_t launch_bin(const ViewCull& v, cudaStream_t stream)
+{
+    if (v.slices == 0) return cudaSuccess;
+    bin_slices_kernel<<<v.slices, kBinWarps * 32, 0, stream>>>(v);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_cull(const ViewCull& v, const CullConfig& cfg, uint32_t* dev_error, cudaStream_t stream)
 {
     if (v.clusters == 0) return cudaSuccess;
-#define CF_DISPATCH(K, W, T, S)                                                                   \
-    if (cfg.clusters_per_warp == K && cfg.warps == W && cfg.tile == T && cfg.stages == S)         \
-        return launch_cull_t<K, W, T, S>(v, dev_error, stream);
+#define CF_DISPATCH(K, W, T, S, B)                                                                              \
+    if (cfg.clusters_per_warp == K && cfg.warps == W && cfg.tile == T && cfg.stages == S && (cfg.binned != 0) == B) \
+        return launch_cull_t<K, W, T, S, B>(v, dev_error, stream);
     CF_CULL_CONFIGS(CF_DISPATCH)
 #undef CF_DISPATCH
     return cudaErrorInvalidValue;
@@ -568,7 +913,10 @@ cudaError_t launch_finalize(const ViewCull& v, cudaStream_t stream)
         if (v.total) return cudaMemsetAsync(v.total, 0, sizeof(uint32_t), stream);
         return cudaSuccess;
     }
-    finalize_kernel<<<(v.clusters + kFinalizeChunk - 1) / kFinalizeChunk, 1024, 0, stream>>>(v);
+    scan_kernel<<<1, kScanThreads, 0, stream>>>(v);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    copy_kernel<<<(v.clusters + kCopyWarps - 1) / kCopyWarps, kCopyWarps * 32, 0, stream>>>(v);
     return cudaGetLastError();
 }
 

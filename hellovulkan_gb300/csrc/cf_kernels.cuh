@@ -26,7 +26,7 @@ namespace cfk {
 
 constexpr uint32_t kLightPad = 32;       // view-space light arrays are padded to this
 constexpr uint32_t kFlagGranule = 256;   // lights per non-finite flag word
-constexpr uint32_t kFinalizeChunk = 2048;  // clusters per finalize CTA
+
 
 // Device error codes (OR-ed into the context's error word).
 constexpr uint32_t kErrFullWaitTimeout = 1u << 0;   // a consumer waited too long for a light tile
@@ -44,11 +44,50 @@ struct ViewCull {
     CfLightCell* cells;
     uint32_t* indices;
     uint32_t* total;  // may be null
+    // binned path: per depth slice, a candidate list of lpad entries
+    float4* slice_lights;
+    uint32_t* slice_idx;
+    uint32_t* slice_count;      // padded length of each slice's list
+    uint32_t* slice_nonfinite;  // 1 when a listed light has a non-finite coordinate
+    // optional work counters (profiling only, null otherwise): [0] sphere-box
+    // tests against slice slabs and warp union boxes, [1] sphere-box tests
+    // against cluster boxes
+    unsigned long long* work;
+    // cluster groups: the clusters one culling CTA owns.  Plain: group b is
+    // [b*gw, min((b+1)*gw, C)); binned: group b is slice b / gps, clusters
+    // [k*XY + (b % gps)*gw, min(.. + gw, (k+1)*XY)).
+    uint32_t* group_sums;     // capped hit count of each group
+    uint32_t* group_offsets;  // exclusive scan of group_sums
     uint32_t lpad;
     uint32_t clusters;
     uint32_t cap;
-    uint32_t pad_;
+    uint32_t slice_clusters;  // X * Y
+    uint32_t slices;          // Z
+    uint32_t group_width;     // gw = warps * clusters per warp (<= 32)
+    uint32_t groups;
+    uint32_t binned;
 };
+
+// First cluster and end of group b (see ViewCull).
+__host__ __device__ inline void group_range(const ViewCull& v, uint32_t b, uint32_t* first, uint32_t* end)
+{
+    if (v.binned) {
+        const uint32_t gps = (v.slice_clusters + v.group_width - 1) / v.group_width;
+        const uint32_t k = b / gps;
+        *first = k * v.slice_clusters + (b % gps) * v.group_width;
+        const uint32_t e = *first + v.group_width, se = (k + 1) * v.slice_clusters;
+        *end = e < se ? e : se;
+    } else {
+        *first = b * v.group_width;
+        const uint32_t e = *first + v.group_width;
+        *end = e < v.clusters ? e : v.clusters;
+    }
+}
+
+inline uint32_t group_count(uint32_t clusters, uint32_t slice_clusters, uint32_t slices, uint32_t gw, bool binned)
+{
+    return binned ? slices * ((slice_clusters + gw - 1) / gw) : (clusters + gw - 1) / gw;
+}
 
 // One culling configuration: clusters per warp, consumer warps per CTA,
 // lights per shared-memory stage, number of stages.
@@ -57,20 +96,25 @@ struct CullConfig {
     int warps;
     int tile;
     int stages;
+    int binned;  // 0: every light against every cluster; 1: slice candidate lists first
 };
 
 // Workspace carve-up for one view (cf_cull_lights).
 struct WorkspaceLayout {
-    size_t vlights, nonfinite, counts, staging, bytes;
+    size_t vlights, nonfinite, counts, staging, group_sums, group_offsets, slice_lights, slice_idx, slice_count,
+        slice_nonfinite, bytes;
 };
-WorkspaceLayout workspace_layout(uint32_t clusters, uint32_t lights, uint32_t cap);
+// Scratch of one view; `groups` = group_count(...) of the configuration used.
+WorkspaceLayout workspace_layout(uint32_t clusters, uint32_t lights, uint32_t cap, uint32_t slices, bool binned,
+                                 uint32_t groups);
 
 bool cull_config_supported(const CullConfig& c);
-CullConfig default_cull_config(uint32_t clusters, uint32_t lights);
+CullConfig default_cull_config(uint32_t clusters, uint32_t lights, uint32_t slices);
 
 cudaError_t launch_aabb(const CfClusterForwardUBO& ubo, CfAABB* aabbs, cudaStream_t stream);
 cudaError_t launch_light_xform(const CfLightData* lights, uint32_t count, const float view[16], float4* vlights,
                                uint32_t* nonfinite, cudaStream_t stream);
+cudaError_t launch_bin(const ViewCull& v, cudaStream_t stream);
 cudaError_t launch_cull(const ViewCull& v, const CullConfig& cfg, uint32_t* dev_error, cudaStream_t stream);
 cudaError_t launch_finalize(const ViewCull& v, cudaStream_t stream);
 

@@ -77,7 +77,14 @@ extern "C" int cf_cull_lights_static_scratch(const CfClusterForwardUBO* ubo, con
     if (index_capacity < (uint64_t)C * cap)
         return fail(CF_ERROR_CAPACITY, "index capacity %llu < clusters x cap = %llu", (unsigned long long)index_capacity,
                     (unsigned long long)C * cap);
-    const cfk::WorkspaceLayout L = cfk::workspace_layout(C, light_count, cap);
+    // the automatic kernel choice when its scratch fits, else the brute-force
+    // kernels, which need less (both give the same result)
+    cfk::CullConfig cfg = choose_config(*ubo, light_count, nullptr);
+    cfk::WorkspaceLayout L = layout_for(*ubo, light_count, cap, cfg);
+    if (L.bytes > kStaticScratchBytes && cfg.binned) {
+        cfg = cfk::default_cull_config(C, light_count, 1);
+        L = layout_for(*ubo, light_count, cap, cfg);
+    }
     if (L.bytes > kStaticScratchBytes)
         return fail(CF_ERROR_CAPACITY,
                     "this view needs %llu bytes of scratch (%u clusters, %u lights, cap %u); the static scratch of "
@@ -95,6 +102,6 @@ extern "C" int cf_cull_lights_static_scratch(const CfClusterForwardUBO* ubo, con
         cudaError_t e = cudaMemsetAsync(err_word, 0, sizeof(uint32_t), st);
         if (e != cudaSuccess) return cuda_fail(e, "clear the static scratch error word");
     }
-    return enqueue_cull(*ubo, d_aabbs, d_lights, light_count, cap, d_cells, d_indices, d_total, ws, err_word, nullptr,
-                        st, nullptr);
+    return enqueue_cull(*ubo, d_aabbs, d_lights, light_count, cap, d_cells, d_indices, d_total, ws, err_word, cfg, st,
+                        nullptr);
 }

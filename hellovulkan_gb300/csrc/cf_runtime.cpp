@@ -103,14 +103,31 @@ int grow(void** ptr, size_t* capacity, size_t bytes, const char* what)
     return CF_SUCCESS;
 }
 
-int enqueue_cull(const CfClusterForwardUBO& ubo, const CfAABB* d_aabbs, const CfLightData* d_lights,
-                 uint32_t light_count, uint32_t cap, CfLightCell* d_cells, uint32_t* d_indices, uint32_t* d_total,
-                 unsigned char* ws, uint32_t* dev_error, const cfk::CullConfig* cfg_override, cudaStream_t stream,
-                 cudaEvent_t* stage_events)
+cfk::CullConfig choose_config(const CfClusterForwardUBO& ubo, uint32_t light_count, const cfk::CullConfig* override_cfg)
+{
+    if (override_cfg) return *override_cfg;
+    const uint32_t C = ubo.sliceCountX * ubo.sliceCountY * ubo.sliceCountZ;
+    return cfk::default_cull_config(C, light_count, ubo.sliceCountZ);
+}
+
+cfk::WorkspaceLayout layout_for(const CfClusterForwardUBO& ubo, uint32_t light_count, uint32_t cap,
+                                const cfk::CullConfig& cfg)
 {
     const uint32_t C = ubo.sliceCountX * ubo.sliceCountY * ubo.sliceCountZ;
-    const cfk::WorkspaceLayout L = cfk::workspace_layout(C, light_count, cap);
+    const uint32_t groups = cfk::group_count(C, ubo.sliceCountX * ubo.sliceCountY, ubo.sliceCountZ,
+                                             (uint32_t)(cfg.warps * cfg.clusters_per_warp), cfg.binned != 0);
+    return cfk::workspace_layout(C, light_count, cap, ubo.sliceCountZ, cfg.binned != 0, groups);
+}
+
+int enqueue_cull(const CfClusterForwardUBO& ubo, const CfAABB* d_aabbs, const CfLightData* d_lights,
+                 uint32_t light_count, uint32_t cap, CfLightCell* d_cells, uint32_t* d_indices, uint32_t* d_total,
+                 unsigned char* ws, uint32_t* dev_error, const cfk::CullConfig& cfg, cudaStream_t stream,
+                 cudaEvent_t* stage_events, unsigned long long* work)
+{
+    const uint32_t C = ubo.sliceCountX * ubo.sliceCountY * ubo.sliceCountZ;
+    const cfk::WorkspaceLayout L = layout_for(ubo, light_count, cap, cfg);
     cfk::ViewCull v{};
+    v.work = work;
     v.vlights = reinterpret_cast<const float4*>(ws + L.vlights);
     v.nonfinite = reinterpret_cast<const uint32_t*>(ws + L.nonfinite);
     v.aabbs = reinterpret_cast<const float4*>(d_aabbs);
@@ -122,15 +139,29 @@ int enqueue_cull(const CfClusterForwardUBO& ubo, const CfAABB* d_aabbs, const Cf
     v.lpad = cfk::pad_lights(light_count);
     v.clusters = C;
     v.cap = cap;
+    v.slice_clusters = ubo.sliceCountX * ubo.sliceCountY;
+    v.slices = ubo.sliceCountZ;
+    v.binned = cfg.binned ? 1u : 0u;
+    v.group_width = (uint32_t)(cfg.warps * cfg.clusters_per_warp);
+    v.groups = cfk::group_count(C, v.slice_clusters, v.slices, v.group_width, cfg.binned != 0);
+    v.group_sums = reinterpret_cast<uint32_t*>(ws + L.group_sums);
+    v.group_offsets = reinterpret_cast<uint32_t*>(ws + L.group_offsets);
+    if (cfg.binned) {
+        v.slice_lights = reinterpret_cast<float4*>(ws + L.slice_lights);
+        v.slice_idx = reinterpret_cast<uint32_t*>(ws + L.slice_idx);
+        v.slice_count = reinterpret_cast<uint32_t*>(ws + L.slice_count);
+        v.slice_nonfinite = reinterpret_cast<uint32_t*>(ws + L.slice_nonfinite);
+    }
     cudaError_t e = stage_events ? cudaEventRecord(stage_events[0], stream) : cudaSuccess;
     if (e == cudaSuccess)
         e = cfk::launch_light_xform(d_lights, light_count, ubo.cameraView,
-                                            reinterpret_cast<float4*>(ws + L.vlights),
-                                            reinterpret_cast<uint32_t*>(ws + L.nonfinite), stream);
+                                    reinterpret_cast<float4*>(ws + L.vlights),
+                                    reinterpret_cast<uint32_t*>(ws + L.nonfinite), stream);
     if (e != cudaSuccess) return cuda_fail(e, "light transform launch");
-    const cfk::CullConfig cfg = cfg_override ? *cfg_override : cfk::default_cull_config(C, light_count);
     if (stage_events) e = cudaEventRecord(stage_events[1], stream);
-    if (e == cudaSuccess) e = cfk::launch_cull(v, cfg, dev_error, stream);
+    if (e == cudaSuccess && cfg.binned) e = cfk::launch_bin(v, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "slice binning launch");
+    e = cfk::launch_cull(v, cfg, dev_error, stream);
     if (e != cudaSuccess) return cuda_fail(e, "light culling launch");
     if (stage_events) e = cudaEventRecord(stage_events[2], stream);
     if (e == cudaSuccess) e = cfk::launch_finalize(v, stream);
@@ -188,6 +219,7 @@ struct CfPipelineLightCulling {
     cfk::CullConfig cfg{};
     bool has_cfg = false;
     cudaEvent_t stage_events[4] = {nullptr, nullptr, nullptr, nullptr};  // stage timing, when enabled
+    unsigned long long* d_work = nullptr;                                   // work counters, when enabled
 };
 
 namespace {
@@ -524,7 +556,38 @@ int cf_pipeline_light_culling_destroy(CfPipelineLightCulling* p)
     DeviceGuard g(p->ctx->device);
     for (cudaEvent_t& e : p->stage_events)
         if (e) cudaEventDestroy(e);
+    cudaFree(p->d_work);
     delete p;
+    return CF_SUCCESS;
+}
+
+int cf_pipeline_light_culling_enable_work_counters(CfPipelineLightCulling* p, int enable)
+{
+    if (!p) return fail(CF_ERROR_INVALID_ARGUMENT, "null pipeline");
+    DeviceGuard g(p->ctx->device);
+    if (!enable) {
+        cudaFree(p->d_work);
+        p->d_work = nullptr;
+        return CF_SUCCESS;
+    }
+    if (p->d_work) return CF_SUCCESS;
+    cudaError_t e = cudaMalloc(&p->d_work, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(p->d_work, 0, 2 * sizeof(unsigned long long));
+    return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "work counters");
+}
+
+int cf_pipeline_light_culling_read_work_counters(CfPipelineLightCulling* p, uint64_t counters[2])
+{
+    if (!p || !counters) return fail(CF_ERROR_INVALID_ARGUMENT, "null argument");
+    if (!p->d_work) return fail(CF_ERROR_NOT_READY, "work counters are not enabled");
+    DeviceGuard g(p->ctx->device);
+    unsigned long long h[2] = {0, 0};
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(h, p->d_work, sizeof(h), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemset(p->d_work, 0, sizeof(h));
+    if (e != cudaSuccess) return cuda_fail(e, "read work counters");
+    counters[0] = h[0];
+    counters[1] = h[1];
     return CF_SUCCESS;
 }
 
@@ -583,26 +646,27 @@ int cf_pipeline_light_culling_fill_command_buffer(CfPipelineLightCulling* p, voi
     if (p->lights->count && !p->lights->d_lights) return fail(CF_ERROR_NOT_READY, "no lights uploaded");
     DeviceGuard g(p->ctx->device);
     if (g.err()) return cuda_fail(g.err(), "cudaSetDevice");
-    const cfk::WorkspaceLayout L = cfk::workspace_layout(r->clusters, p->lights->count, r->cap);
+    const cfk::CullConfig cfg = choose_config(p->ubo, p->lights->count, p->has_cfg ? &p->cfg : nullptr);
+    const cfk::WorkspaceLayout L = layout_for(p->ubo, p->lights->count, r->cap, cfg);
     int s = grow(reinterpret_cast<void**>(&r->d_ws), &r->ws_capacity, L.bytes, "culling workspace");
     if (s) return s;
     return enqueue_cull(p->ubo, r->d_aabbs, p->lights->d_lights, p->lights->count, r->cap, r->d_cells, r->d_indices,
-                        r->d_total, r->d_ws, p->ctx->dev_error, p->has_cfg ? &p->cfg : nullptr, (cudaStream_t)stream,
-                        p->stage_events[0] ? p->stage_events : nullptr);
+                        r->d_total, r->d_ws, p->ctx->dev_error, cfg, (cudaStream_t)stream,
+                        p->stage_events[0] ? p->stage_events : nullptr, p->d_work);
 }
 
-int cf_pipeline_light_culling_set_tuning(CfPipelineLightCulling* p, int clusters_per_warp, int warps,
-                                                    int tile, int stages)
+int cf_pipeline_light_culling_set_tuning(CfPipelineLightCulling* p, int clusters_per_warp, int warps, int tile,
+                                         int stages, int binned)
 {
     if (!p) return fail(CF_ERROR_INVALID_ARGUMENT, "null pipeline");
     if (clusters_per_warp == 0) {
         p->has_cfg = false;
         return CF_SUCCESS;
     }
-    const cfk::CullConfig c{clusters_per_warp, warps, tile, stages};
+    const cfk::CullConfig c{clusters_per_warp, warps, tile, stages, binned ? 1 : 0};
     if (!cfk::cull_config_supported(c))
-        return fail(CF_ERROR_INVALID_ARGUMENT, "no culling kernel for K=%d warps=%d tile=%d stages=%d", clusters_per_warp,
-                    warps, tile, stages);
+        return fail(CF_ERROR_INVALID_ARGUMENT, "no culling kernel for K=%d warps=%d tile=%d stages=%d binned=%d",
+                    clusters_per_warp, warps, tile, stages, binned);
     p->cfg = c;
     p->has_cfg = true;
     return CF_SUCCESS;
@@ -621,10 +685,13 @@ int cf_cull_workspace_device_error(void* d_workspace, uint32_t* device_error)
     return v ? fail(CF_ERROR_DEVICE_TIMEOUT, "device error word 0x%x", v) : CF_SUCCESS;
 }
 
-int cf_cull_workspace_size(uint32_t cluster_count, uint32_t light_count, uint32_t cap, uint64_t* bytes)
+int cf_cull_workspace_size(const CfClusterForwardUBO* ubo, uint32_t light_count, uint32_t cap, uint64_t* bytes)
 {
-    if (!bytes) return fail(CF_ERROR_INVALID_ARGUMENT, "null argument");
-    *bytes = cfk::workspace_layout(cluster_count, light_count, cap).bytes;
+    if (!ubo || !bytes) return fail(CF_ERROR_INVALID_ARGUMENT, "cf_cull_workspace_size: null argument");
+    uint32_t C = 0;
+    int s = validate_grid(ubo->sliceCountX, ubo->sliceCountY, ubo->sliceCountZ, cap, &C);
+    if (s) return s;
+    *bytes = layout_for(*ubo, light_count, cap, choose_config(*ubo, light_count, nullptr)).bytes;
     return CF_SUCCESS;
 }
 
@@ -654,13 +721,14 @@ int cf_cull_lights(const CfClusterForwardUBO* ubo, const CfAABB* d_aabbs, const 
     if (index_capacity < (uint64_t)C * cap)
         return fail(CF_ERROR_CAPACITY, "index capacity %llu < clusters x cap = %llu", (unsigned long long)index_capacity,
                     (unsigned long long)C * cap);
-    const cfk::WorkspaceLayout L = cfk::workspace_layout(C, light_count, cap);
+    const cfk::CullConfig cfg = choose_config(*ubo, light_count, nullptr);
+    const cfk::WorkspaceLayout L = layout_for(*ubo, light_count, cap, cfg);
     if (workspace_bytes < L.bytes)
         return fail(CF_ERROR_CAPACITY, "workspace %llu bytes < %llu needed", (unsigned long long)workspace_bytes,
                     (unsigned long long)L.bytes);
     unsigned char* ws = static_cast<unsigned char*>(d_workspace);
     return enqueue_cull(*ubo, d_aabbs, d_lights, light_count, cap, d_cells, d_indices, d_total, ws,
-                        reinterpret_cast<uint32_t*>(ws), nullptr, (cudaStream_t)stream, nullptr);
+                        reinterpret_cast<uint32_t*>(ws), cfg, (cudaStream_t)stream, nullptr);
 }
 
 }  // extern "C"

@@ -35,10 +35,16 @@ private:
 // Ensures *ptr holds at least `bytes` of zero-filled device memory.
 int grow(void** ptr, size_t* capacity, size_t bytes, const char* what);
 
-// Light transform + culling + offset scan of one view on `stream`.
+// The culling configuration for a view: the override, else the automatic choice.
+cfk::CullConfig choose_config(const CfClusterForwardUBO& ubo, uint32_t light_count,
+                              const cfk::CullConfig* override_cfg);
+cfk::WorkspaceLayout layout_for(const CfClusterForwardUBO& ubo, uint32_t light_count, uint32_t cap,
+                                const cfk::CullConfig& cfg);
+
+// Light transform (+ slice binning) + culling + offset scan of one view on `stream`.
 int enqueue_cull(const CfClusterForwardUBO& ubo, const CfAABB* d_aabbs, const CfLightData* d_lights,
                  uint32_t light_count, uint32_t cap, CfLightCell* d_cells, uint32_t* d_indices, uint32_t* d_total,
-                 unsigned char* ws, uint32_t* dev_error, const cfk::CullConfig* cfg_override, cudaStream_t stream,
-                 cudaEvent_t* stage_events);
+                 unsigned char* ws, uint32_t* dev_error, const cfk::CullConfig& cfg, cudaStream_t stream,
+                 cudaEvent_t* stage_events, unsigned long long* work = nullptr);
 
 }  // namespace cfrt

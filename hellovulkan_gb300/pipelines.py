@@ -161,15 +161,25 @@ class PipelineLightCulling:
     def set_cluster_forward_ubo(self, ubo: CfClusterForwardUBO) -> None:
         check(lib().cf_pipeline_light_culling_set_cluster_forward_ubo(self.handle, C.byref(ubo)))
 
-    def set_tuning(self, clusters_per_warp: int = 0, warps: int = 0, tile: int = 0, stages: int = 0) -> None:
-        """Selects a culling kernel configuration (0 = automatic)."""
-        check(lib().cf_pipeline_light_culling_set_tuning(self.handle, clusters_per_warp, warps, tile, stages))
+    def set_tuning(self, clusters_per_warp: int = 0, warps: int = 0, tile: int = 0, stages: int = 0,
+                   binned: int = 0) -> None:
+        """Selects a culling kernel configuration (clusters_per_warp 0 = automatic)."""
+        check(lib().cf_pipeline_light_culling_set_tuning(self.handle, clusters_per_warp, warps, tile, stages, binned))
 
     def fill_command_buffer(self, stream=None) -> None:
         check(lib().cf_pipeline_light_culling_fill_command_buffer(self.handle, stream_handle(stream)))
 
     def enable_stage_timing(self, enable: bool = True) -> None:
         check(lib().cf_pipeline_light_culling_enable_stage_timing(self.handle, int(enable)))
+
+    def enable_work_counters(self, enable: bool = True) -> None:
+        check(lib().cf_pipeline_light_culling_enable_work_counters(self.handle, int(enable)))
+
+    def read_work_counters(self):
+        """(slab/union-box tests, cluster-box tests) executed since the last read."""
+        out = (C.c_uint64 * 2)()
+        check(lib().cf_pipeline_light_culling_read_work_counters(self.handle, out))
+        return int(out[0]), int(out[1])
 
     def stage_times_ms(self):
         """(light transform, culling, offset scan) of the last call, in ms."""

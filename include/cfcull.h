@@ -174,10 +174,13 @@ CFCULL_API int cf_pipeline_light_culling_set_cluster_forward_ubo(CfPipelineLight
 CFCULL_API int cf_pipeline_light_culling_fill_command_buffer(CfPipelineLightCulling* pipe, void* stream);
 
 /* Tuning: selects the culling kernel configuration (clusters per warp,
- * consumer warps per CTA, lights per shared-memory stage, stages); all zero
- * restores the automatic choice.  Unsupported combinations are rejected. */
+ * consumer warps per CTA, lights per shared-memory stage, stages, and
+ * binned = 1 for the depth-slice candidate lists or 0 for every light against
+ * every cluster); clusters_per_warp = 0 restores the automatic choice.
+ * Unsupported combinations are rejected.  Every configuration gives the same
+ * output. */
 CFCULL_API int cf_pipeline_light_culling_set_tuning(CfPipelineLightCulling* pipe, int clusters_per_warp, int warps,
-                                                    int tile, int stages);
+                                                    int tile, int stages, int binned);
 /* Stage timing, the counterpart of the reference's Tracy GPU zone
  * "Light_Culling" (PipelineLightCulling.cpp:53): when enabled, each
  * fill_command_buffer records CUDA events around its three kernels, and
@@ -185,14 +188,21 @@ CFCULL_API int cf_pipeline_light_culling_set_tuning(CfPipelineLightCulling* pipe
  * offset-scan durations in milliseconds (waits for them). */
 CFCULL_API int cf_pipeline_light_culling_enable_stage_timing(CfPipelineLightCulling* pipe, int enable);
 CFCULL_API int cf_pipeline_light_culling_get_stage_times(CfPipelineLightCulling* pipe, float ms[3]);
+/* Work counters for profiling: when enabled, the kernels add up the
+ * sphere-box tests they execute — counters[0] against depth-slice slabs and
+ * per-warp union boxes, counters[1] against cluster boxes.  read returns the
+ * sums since the last read and clears them (synchronises the device). */
+CFCULL_API int cf_pipeline_light_culling_enable_work_counters(CfPipelineLightCulling* pipe, int enable);
+CFCULL_API int cf_pipeline_light_culling_read_work_counters(CfPipelineLightCulling* pipe, uint64_t counters[2]);
 
 /* ------------------------------------------------------------------------ */
 /* Stateless entry points on caller-owned device memory.                     */
 /* ------------------------------------------------------------------------ */
 
-/* Bytes of device workspace cf_cull_lights needs. */
-CFCULL_API int cf_cull_workspace_size(uint32_t cluster_count, uint32_t light_count, uint32_t max_lights_per_cluster,
-                                      uint64_t* bytes);
+/* Bytes of device workspace cf_cull_lights needs for a view of this grid
+ * (ubo: host pointer) and light count. */
+CFCULL_API int cf_cull_workspace_size(const CfClusterForwardUBO* ubo, uint32_t light_count,
+                                      uint32_t max_lights_per_cluster, uint64_t* bytes);
 /* AABBGenerator.comp over the grid of `ubo` (host pointer) into
  * d_aabbs[X*Y*Z] (device). */
 CFCULL_API int cf_generate_aabbs(const CfClusterForwardUBO* ubo, CfAABB* d_aabbs, void* stream);

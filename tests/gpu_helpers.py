@@ -53,7 +53,7 @@ def run_stateless(view, stream=None):
     idx = torch.empty(Cn * cap, dtype=torch.int32, device="cuda")
     total = torch.zeros(1, dtype=torch.int32, device="cuda")
     n = C.c_uint64()
-    check(L.cf_cull_workspace_size(Cn, view.light_count, cap, C.byref(n)))
+    check(L.cf_cull_workspace_size(C.byref(view.ubo), view.light_count, cap, C.byref(n)))
     ws = torch.zeros(n.value, dtype=torch.uint8, device="cuda")
     s = (stream or torch.cuda.current_stream()).cuda_stream
     check(L.cf_generate_aabbs(C.byref(view.ubo), aabbs.data_ptr(), s))

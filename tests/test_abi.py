@@ -61,10 +61,15 @@ def test_status_strings_and_argument_errors_without_gpu(cflib):
     assert L.cf_generate_aabbs(None, None, None) == 1
     assert b"null" in L.cf_last_error_message()
     n = C.c_uint64()
-    assert L.cf_cull_workspace_size(3456, 1024, 150, C.byref(n)) == 0
-    # status block + lights + flags + counts + staging, each 256-byte aligned
+    from hellovulkan_gb300 import scenes
+    v = scenes.plain_small(1)
+    assert L.cf_cull_workspace_size(C.byref(v.ubo), 1024, 150, C.byref(n)) == 0
+    # status block + lights + flags + counts + staging + group sums and offsets
+    # (24 slices x 9 groups of 16 clusters) + 24 slice candidate lists
+    # (float4 + index) + slice counts + slice flags, each 256-byte aligned
     al = lambda x: (x + 255) // 256 * 256
-    assert n.value == 256 + al(1024 * 16) + al(4 * 4) + al(3456 * 4) + al(3456 * 150 * 4)
+    assert n.value == (256 + al(1024 * 16) + al(4 * 4) + al(3456 * 4) + al(3456 * 150 * 4) + 2 * al(216 * 4)
+                       + al(24 * 1024 * 16) + al(24 * 1024 * 4) + 2 * al(24 * 4))
     ubo = _lib.CfClusterForwardUBO()
     ubo.sliceCountX, ubo.sliceCountY, ubo.sliceCountZ = 0, 9, 24
     assert L.cf_generate_aabbs(C.byref(ubo), C.c_void_p(256), None) == 1

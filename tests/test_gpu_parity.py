@@ -10,7 +10,7 @@ from hellovulkan_gb300.camera import look_at_rh, ubo_from_bytes
 
 pytestmark = pytest.mark.gpu
 
-TUNINGS = [(1, 4, 512, 4), (2, 4, 512, 4), (4, 4, 512, 4), (1, 8, 512, 4), (2, 8, 512, 4), (4, 8, 512, 4)]
+TUNINGS = [(k, w, 512, 4, 0) for k in (1, 2, 4) for w in (4, 8)] + [(k, w, 256, 4, 1) for k in (1, 2, 4) for w in (4, 8)]
 
 
 def golden_views(golden):

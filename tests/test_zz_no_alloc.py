@@ -51,7 +51,7 @@ def _with_workspace(view, aabbs, lights):
     from hellovulkan_gb300._lib import check, lib
     cells, idx, total = _outputs(view)
     nbytes = C.c_uint64()
-    check(lib().cf_cull_workspace_size(view.clusters, view.light_count, view.cap, C.byref(nbytes)))
+    check(lib().cf_cull_workspace_size(C.byref(view.ubo), view.light_count, view.cap, C.byref(nbytes)))
     ws = torch.zeros(nbytes.value, dtype=torch.uint8, device="cuda")
     check(lib().cf_cull_lights(C.byref(view.ubo), aabbs.data_ptr(), lights.data_ptr(), view.light_count, view.cap,
                                cells.data_ptr(), idx.data_ptr(), view.clusters * view.cap, total.data_ptr(),

@@ -61,6 +61,7 @@ def parse():
     p.add_argument("--workload", choices=["plain_large", "plain_small"], default="plain_large")
     p.add_argument("--tuning", type=str, default="", help="K,warps,tile,stages,binned of the culling kernel")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-batch", action="store_true", help="skip the 256-view batched measurement")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline budget")
     return p.parse_args()
 
@@ -214,6 +215,94 @@ def run_reference_arm(args):
 
 
 # --------------------------------------------------------------------------- GPU side
+def measure_batch(ctx, stream, n_views=256, passes=20, seed=3, sample_views=6):
+    """The batched form on the 256-view uneven mix (grids 8x8x16 .. 32x18x48,
+    256..65536 blob lights each): one pass culls every view (a CUDA-graph
+    replay of the batched launches, autotuned per grid), against the same views
+    culled one after another with one launch sequence per view
+    (cf_cull_lights).  Inputs (lights, AABBs, outputs) exceed the L2, so no
+    flush is needed between passes."""
+    import ctypes as C
+
+    import torch
+
+    from hellovulkan_gb300 import scenes
+    from hellovulkan_gb300._lib import check, lib
+    from hellovulkan_gb300.batch import Batch, BatchBuffers
+
+    views = scenes.batch_mix(seed, n_views)
+    bufs = BatchBuffers(views)
+    b = Batch(ctx)
+    b.set_views(bufs.batch_views())
+    b.generate_aabbs(stream)
+    t0 = time.perf_counter()
+    b.autotune(2, stream)
+    tune_s = time.perf_counter() - t0
+
+    def timed(fn, n):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        for s, e in ev:
+            s.record(stream)
+            fn()
+            e.record(stream)
+        torch.cuda.synchronize()
+        return [s.elapsed_time(e) for s, e in ev]
+
+    for _ in range(3):
+        b.cull(stream)
+    batch_ms = timed(lambda: b.cull(stream), passes)
+
+    L = lib()
+    sizes = []
+    for v in views:
+        nb = C.c_uint64()
+        check(L.cf_cull_workspace_size(C.byref(v.ubo), v.light_count, v.cap, C.byref(nb)))
+        sizes.append(nb.value)
+    ws = torch.zeros(max(sizes), dtype=torch.uint8, device="cuda")
+    sh = stream.cuda_stream
+
+    def per_view_pass():
+        for i, v in enumerate(views):
+            check(L.cf_cull_lights(C.byref(v.ubo), bufs.aabbs[i].data_ptr(),
+                                   bufs.lights[i].data_ptr() if v.light_count else None, v.light_count, v.cap,
+                                   bufs.cells[i].data_ptr(), bufs.indices[i].data_ptr(), v.clusters * v.cap,
+                                   bufs.totals[i].data_ptr(), ws.data_ptr(), ws.numel(), sh))
+
+    per_view_pass()
+    per_view_ms = timed(per_view_pass, 3)
+    b.cull(stream)  # leave the batch's own outputs in the buffers for the parity check
+    torch.cuda.synchronize()
+
+    from oracle import Oracle
+    o = Oracle()
+    order = sorted(range(n_views), key=lambda i: views[i].light_count)
+    sample = sorted({order[0], order[-1], order[n_views // 2]} | set(
+        np.random.default_rng(seed).choice(n_views, sample_views - 3, replace=False).tolist()))
+    parity = True
+    for i in sample:
+        a, cells, idx = bufs.read(i)
+        oa = o.generate_aabbs(views[i].ubo)
+        oc, oi, _ = o.cull(views[i].ubo, oa, views[i].lights, views[i].cap)
+        parity &= bool(np.array_equal(a.view(np.uint32), oa.view(np.uint32)) and np.array_equal(cells, oc)
+                       and np.array_equal(idx, oi))
+    tests = sum(v.clusters * v.light_count for v in views)
+    bm, pm = float(np.mean(batch_ms)), float(np.mean(per_view_ms))
+    info = b.info()
+    b.close()
+    return {
+        "workload": "%d views, grids {8x8x16,16x9x24,24x14x32,32x18x48}, %d..%d lights (total %d), cap 150, "
+                    "seed %d" % (n_views, min(v.light_count for v in views), max(v.light_count for v in views),
+                                 sum(v.light_count for v in views), seed),
+        "ms_per_batch": bm, "views_per_s": n_views / (bm * 1e-3),
+        "tests_per_s": tests / (bm * 1e-3),
+        "per_view_launch_ms": pm, "per_view_launch_views_per_s": n_views / (pm * 1e-3),
+        "speedup_vs_per_view_launch": pm / bm,
+        "passes": passes, "graph": True, "autotune_s": tune_s, "buckets": info["bucket_configs"],
+        "items": info["items"], "parity_sampled_views": parity, "sampled_views": sample,
+        "l2": "inputs larger than L2 (%.0f MB of buffers), no flush" % (bufs.device_bytes / 1e6),
+    }
+
+
 def run_ours(args):
     import torch
 
@@ -320,6 +409,10 @@ def run_ours(args):
     cull.set_tuning(0)
     cull.enable_stage_timing(False)
 
+    batched = None
+    if not args.no_batch and rank == 0:
+        batched = measure_batch(ctx, stream)
+
     tests_per_view = view.clusters * view.light_count
     stats = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device="cuda")
     if ws > 1:
@@ -407,6 +500,7 @@ def run_ours(args):
                 "timing": "host clock, synchronised, pinned host buffers"},
         "gpu_launches": 4 * (args.steps + e2e_steps),
         "clocks": clocks,
+        "batched": batched,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:

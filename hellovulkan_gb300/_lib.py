@@ -57,6 +57,32 @@ class CfClusterForwardBuffers(C.Structure):
     ]
 
 
+class CfBatchView(C.Structure):
+    _fields_ = [
+        ("ubo", CfClusterForwardUBO),
+        ("d_lights", C.c_void_p),
+        ("d_aabbs", C.c_void_p),
+        ("d_cells", C.c_void_p),
+        ("d_indices", C.c_void_p),
+        ("d_total", C.c_void_p),
+        ("index_capacity", C.c_uint64),
+        ("light_count", C.c_uint32),
+        ("max_lights_per_cluster", C.c_uint32),
+        ("_pad", C.c_uint32 * 2),
+    ]
+
+
+class CfBatchInfo(C.Structure):
+    _fields_ = [
+        ("views", C.c_uint32), ("items", C.c_uint32), ("buckets", C.c_uint32), ("_pad", C.c_uint32),
+        ("workspace_bytes", C.c_uint64),
+        ("bucket_slice_clusters", C.c_uint32 * 8),
+        ("bucket_config", (C.c_int32 * 4) * 8),
+        ("bucket_ctas", C.c_int32 * 8),
+    ]
+
+
+assert C.sizeof(CfBatchView) == 240 and C.sizeof(CfBatchInfo) == 216
 assert C.sizeof(CfLightData) == 48 and C.sizeof(CfAABB) == 32 and C.sizeof(CfLightCell) == 8
 assert C.sizeof(CfClusterForwardUBO) == 176
 
@@ -121,6 +147,16 @@ _SIGS = {
     "cf_cull_lights": [C.POINTER(CfClusterForwardUBO), _P, _P, _U32, _U32, _P, _P, _U64, _P, _P, _U64, _P],
     "cf_cull_workspace_device_error": [_P, _PU32],
     "cf_cull_lights_static_scratch": [C.POINTER(CfClusterForwardUBO), _P, _P, _U32, _U32, _P, _P, _U64, _P, _P, _P],
+    "cf_batch_create": [_P, C.POINTER(_P)],
+    "cf_batch_destroy": [_P],
+    "cf_batch_set_views": [_P, C.POINTER(CfBatchView), _U32],
+    "cf_batch_update_view_matrices": [_P, C.POINTER(CfClusterForwardUBO), _U32, _P],
+    "cf_batch_generate_aabbs": [_P, _P],
+    "cf_batch_cull": [_P, _P],
+    "cf_batch_set_graph": [_P, _I],
+    "cf_batch_set_tuning": [_P, _U32, _I, _I, _I, _I],
+    "cf_batch_autotune": [_P, _I, _P],
+    "cf_batch_get_info": [_P, C.POINTER(CfBatchInfo)],
 }
 _RESTYPE = {"cf_status_string": C.c_char_p, "cf_last_error_message": C.c_char_p}
 

@@ -83,7 +83,10 @@ def ubo_to_bytes(u: CfClusterForwardUBO) -> np.ndarray:
 
 
 def ubo_from_bytes(b) -> CfClusterForwardUBO:
-    return CfClusterForwardUBO.from_buffer_copy(bytes(np.asarray(b, np.uint8)))
+    """A UBO from its 176 bytes (bytes, or a uint8 array as stored in fixtures)."""
+    if not isinstance(b, (bytes, bytearray)):
+        b = np.asarray(b, np.uint8).tobytes()
+    return CfClusterForwardUBO.from_buffer_copy(bytes(b))
 
 
 def ubo_grid(u: CfClusterForwardUBO):

@@ -200,26 +200,60 @@ struct Mat4 {
     float m[16];
 };
 
-__global__ void __launch_bounds__(kFlagGranule) light_xform_kernel(const CfLightData* __restrict__ lights,
-                                                                   uint32_t count, uint32_t lpad, const Mat4 view,
-                                                                   float4* __restrict__ out,
-                                                                   uint32_t* __restrict__ nonfinite)
+// Granule blk (256 lights) of one view; every thread of the block takes part.
+__device__ __forceinline__ void light_xform_body(const CfLightData* __restrict__ lights, uint32_t count,
+                                                 uint32_t lpad, const float* view, float4* __restrict__ out,
+                                                 uint32_t* __restrict__ nonfinite, uint32_t blk)
 {
-    const uint32_t i = blockIdx.x * kFlagGranule + threadIdx.x;
+    const uint32_t i = blk * kFlagGranule + threadIdx.x;
     bool bad = false;
     if (i < count) {
         const float4 p = __ldg(reinterpret_cast<const float4*>(&lights[i].position[0]));
         const float r = __ldg(&lights[i].radius);
-        const float x = cf_mat4_row(view.m, 0, p.x, p.y, p.z, p.w);
-        const float y = cf_mat4_row(view.m, 1, p.x, p.y, p.z, p.w);
-        const float z = cf_mat4_row(view.m, 2, p.x, p.y, p.z, p.w);
+        const float x = cf_mat4_row(view, 0, p.x, p.y, p.z, p.w);
+        const float y = cf_mat4_row(view, 1, p.x, p.y, p.z, p.w);
+        const float z = cf_mat4_row(view, 2, p.x, p.y, p.z, p.w);
         bad = !(finite_bits(x) && finite_bits(y) && finite_bits(z));
         out[i] = make_float4(x, y, z, cf_fmul(r, r));
     } else if (i < lpad) {
         out[i] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0xff800000u));  // never hits
     }
     const int any_bad = __syncthreads_or(bad);
-    if (threadIdx.x == 0) nonfinite[blockIdx.x] = any_bad ? 1u : 0u;
+    if (threadIdx.x == 0) nonfinite[blk] = any_bad ? 1u : 0u;
+}
+
+__global__ void __launch_bounds__(kFlagGranule) light_xform_kernel(const CfLightData* __restrict__ lights,
+                                                                   uint32_t count, uint32_t lpad, const Mat4 view,
+                                                                   float4* __restrict__ out,
+                                                                   uint32_t* __restrict__ nonfinite)
+{
+    light_xform_body(lights, count, lpad, view.m, out, nonfinite, blockIdx.x);
+}
+
+// Index of the view whose range [prefix[v], prefix[v+1]) holds block b.
+__device__ __forceinline__ uint32_t find_view(const uint32_t* __restrict__ prefix, uint32_t n_views, uint32_t b)
+{
+    uint32_t lo = 0, hi = n_views;  // prefix[lo] <= b < prefix[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&prefix[mid]) <= b) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Batched light transform: block b is granule b - prefix[v] of view v.  Block
+// 0 also resets the culling work queue of the same batch.
+__global__ void __launch_bounds__(kFlagGranule) batch_xform_kernel(const ViewJob* __restrict__ jobs,
+                                                                   const uint32_t* __restrict__ prefix,
+                                                                   uint32_t n_views, uint32_t* __restrict__ queues,
+                                                                   uint32_t n_queues)
+{
+    if (blockIdx.x == 0 && threadIdx.x < n_queues) queues[threadIdx.x] = 0;
+    const uint32_t vi = find_view(prefix, n_views, blockIdx.x);
+    const ViewJob& j = jobs[vi];
+    light_xform_body(j.lights, j.light_count, j.v.lpad, j.view, const_cast<float4*>(j.v.vlights),
+                     const_cast<uint32_t*>(j.v.nonfinite), blockIdx.x - __ldg(&prefix[vi]));
 }
 
 // ---------------------------------------------------------------------------
@@ -336,30 +370,74 @@ __device__ __forceinline__ bool tile_has_nonfinite(const uint32_t* __restrict__ 
     return f != 0;
 }
 
-// blockDim = (WARPS + 1) * 32: warps 0..WARPS-1 consume, warp WARPS produces.
-// Dynamic shared memory: STAGES x TILE float4 (and, binned, STAGES x TILE
-// light indices), then the full/empty mbarriers, the per-stage stop flags and
-// the done-warp counter.
-//   plain   CTA b owns clusters [b*W*K, (b+1)*W*K) and streams every light
-//   binned  CTA b owns group g of slice k (b = k * groups_per_slice + g) and
-//           streams that slice's candidate list made by bin_slices_kernel
+// Shared-memory carve-up of the culling kernels (dynamic shared memory):
+// STAGES x TILE float4 tiles, (binned) STAGES x TILE light indices, the
+// full/empty mbarriers, per-stage stop flags, the done-warp counter, then
+// (binned) the survivor buffer, per-chunk counts, per-warp union boxes and
+// the consumers' abort flag.
 template <int K, int WARPS, int TILE, int STAGES, bool kBinned>
-__global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v, uint32_t* __restrict__ dev_error)
-{
-    static_assert(TILE % 32 == 0, "tiles hold whole warps of lights");
-    extern __shared__ __align__(128) unsigned char smem[];
-    float4* tiles = reinterpret_cast<float4*>(smem);
-    uint32_t* idx_tiles = reinterpret_cast<uint32_t*>(smem + (size_t)STAGES * TILE * sizeof(float4));
-    unsigned char* tail = smem + (size_t)STAGES * TILE * (sizeof(float4) + (kBinned ? sizeof(uint32_t) : 0));
-    uint64_t* full = reinterpret_cast<uint64_t*>(tail);
-    uint64_t* empty = full + STAGES;
-    volatile uint32_t* stop = reinterpret_cast<volatile uint32_t*>(empty + STAGES);
-    uint32_t* done_warps = reinterpret_cast<uint32_t*>(empty + STAGES) + STAGES;
-    // binned only: survivor buffer, per-chunk counts, per-warp union boxes, abort flag
-    unsigned char* binned_extra =
-        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(done_warps + 1) + 15) & ~uintptr_t(15));
-    (void)binned_extra;
+struct CullSmem {
+    float4* tiles;
+    uint32_t* idx_tiles;
+    uint64_t* full;
+    uint64_t* empty;
+    volatile uint32_t* stop;
+    uint32_t* done_warps;
+    unsigned char* binned_extra;
 
+    static constexpr size_t extra_bytes()
+    {
+        return kBinned ? 16 + (size_t)TILE * (sizeof(float4) + sizeof(uint32_t)) + (TILE / 32) * 4 +
+                             (size_t)WARPS * 8 * sizeof(float) + sizeof(uint32_t)
+                       : 0;
+    }
+    static constexpr size_t bytes()
+    {
+        return (size_t)STAGES * TILE * (sizeof(float4) + (kBinned ? sizeof(uint32_t) : 0)) +
+               2 * STAGES * sizeof(uint64_t) + (STAGES + 1) * sizeof(uint32_t) + extra_bytes();
+    }
+    __device__ explicit CullSmem(unsigned char* smem)
+    {
+        tiles = reinterpret_cast<float4*>(smem);
+        idx_tiles = reinterpret_cast<uint32_t*>(smem + (size_t)STAGES * TILE * sizeof(float4));
+        unsigned char* tail = smem + (size_t)STAGES * TILE * (sizeof(float4) + (kBinned ? sizeof(uint32_t) : 0));
+        full = reinterpret_cast<uint64_t*>(tail);
+        empty = full + STAGES;
+        stop = reinterpret_cast<volatile uint32_t*>(empty + STAGES);
+        done_warps = reinterpret_cast<uint32_t*>(empty + STAGES) + STAGES;
+        binned_extra =
+            reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(done_warps + 1) + 15) & ~uintptr_t(15));
+    }
+    __device__ void init()
+    {
+        if (threadIdx.x == 0) {
+            for (int s = 0; s < STAGES; ++s) {
+                mbar_init(smem_u32(&full[s]), 1);
+                mbar_init(smem_u32(&empty[s]), WARPS);
+                stop[s] = 0;
+            }
+            mbar_init_fence();
+        }
+    }
+};
+
+// Culls cluster group `group` of view v with the whole CTA.
+//   plain   the group is clusters [group*W*K, (group+1)*W*K) and the CTA streams
+//           every light of the view
+//   binned  the group is group (group % gps) of slice (group / gps) and the CTA
+//           streams that slice's candidate list made by bin_slices_kernel
+// Tiles are numbered across all groups a CTA culls: tile t of this group is
+// tile seq + t of the CTA, which fixes its stage and mbarrier phases, so the
+// stages keep cycling from one group to the next.  Every tile used (including
+// one that only carries the stop signal) completes one full phase and one
+// empty phase; the number used is returned in *used (valid in every thread
+// after the caller's __syncthreads).  On a timed-out wait the CTA's abort flag
+// is set and the kernel ends after the current group.
+template <int K, int WARPS, int TILE, int STAGES, bool kBinned>
+__device__ __forceinline__ void cull_group(const ViewCull& v, uint32_t group, CullSmem<K, WARPS, TILE, STAGES, kBinned>& sm,
+                                           uint32_t seq, volatile uint32_t* used, volatile uint32_t* abort_flag,
+                                           uint32_t* __restrict__ dev_error)
+{
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const float4* src = v.vlights;
     const uint32_t* src_idx = nullptr;
@@ -367,7 +445,7 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
     bool slice_exact = false;
     if (kBinned) {
         const uint32_t xy = v.slice_clusters, gps = (xy + WARPS * K - 1) / (WARPS * K);
-        const uint32_t k = blockIdx.x / gps, g = blockIdx.x % gps;
+        const uint32_t k = group / gps, g = group % gps;
         src = v.slice_lights + (size_t)k * v.lpad;
         src_idx = v.slice_idx + (size_t)k * v.lpad;
         nsrc = v.slice_count[k];
@@ -375,34 +453,32 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
         first = k * xy + g * (uint32_t)(WARPS * K);
         cl_end = (k + 1) * xy;
     } else {
-        first = blockIdx.x * (uint32_t)(WARPS * K);
+        first = group * (uint32_t)(WARPS * K);
         cl_end = v.clusters;
     }
     const uint32_t ntiles = (nsrc + TILE - 1) / TILE;
-
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < STAGES; ++s) {
-            mbar_init(smem_u32(&full[s]), 1);
-            mbar_init(smem_u32(&empty[s]), WARPS);
-            stop[s] = 0;
-        }
-        *done_warps = 0;
-        mbar_init_fence();
-    }
-    __syncthreads();
+    float4* const tiles = sm.tiles;
+    uint32_t* const idx_tiles = sm.idx_tiles;
+    uint64_t* const full = sm.full;
+    uint64_t* const empty = sm.empty;
+    volatile uint32_t* const stop = sm.stop;
+    uint32_t* const done_warps = sm.done_warps;
 
     if (warp == WARPS) {
         // Producer: one lane streams the tiles through the ring of stages.
         if (lane == 0) {
-            for (uint32_t t = 0; t < ntiles; ++t) {
-                const uint32_t s = t % STAGES;
-                if (t >= STAGES && !mbar_wait_bounded(smem_u32(&empty[s]), ((t / STAGES) & 1u) ^ 1u)) {
+            uint32_t t = 0;
+            for (; t < ntiles; ++t) {
+                const uint32_t g = seq + t, s = g % STAGES;
+                if (g >= STAGES && !mbar_wait_bounded(smem_u32(&empty[s]), ((g / STAGES) & 1u) ^ 1u)) {
                     atomicOr(dev_error, kErrEmptyWaitTimeout);
+                    *abort_flag = 1;
                     break;
                 }
                 if (*reinterpret_cast<volatile uint32_t*>(done_warps) >= (uint32_t)WARPS) {
                     stop[s] = 1;  // every consumer is capped: release them without data
                     mbar_arrive(smem_u32(&full[s]));
+                    ++t;
                     break;
                 }
                 stop[s] = 0;
@@ -415,6 +491,7 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
                     bulk_copy_g2s(smem_u32(idx_tiles + (size_t)s * TILE), src_idx + (size_t)t * TILE,
                                   n * (uint32_t)sizeof(uint32_t), smem_u32(&full[s]));
             }
+            *used = t;
         }
         return;
     }
@@ -467,7 +544,7 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
         // and every warp then tests only the survivors against its K boxes.
         constexpr uint32_t kChunks = TILE / 32;
         constexpr int kPer = (int)((kChunks + WARPS - 1) / WARPS);
-        float4* surv_l = reinterpret_cast<float4*>(binned_extra);
+        float4* surv_l = reinterpret_cast<float4*>(sm.binned_extra);
         uint32_t* surv_i = reinterpret_cast<uint32_t*>(surv_l + TILE);
         uint32_t* s_cnt = surv_i + TILE;
         float* s_box = reinterpret_cast<float*>(s_cnt + kChunks);
@@ -491,13 +568,21 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
         }
         const uint32_t lt_mask = (1u << lane) - 1u;
         for (uint32_t t = 0; t < ntiles; ++t) {
-            const uint32_t s = t % STAGES;
-            if (!mbar_wait_bounded(smem_u32(&full[s]), (t / STAGES) & 1u) && lane == 0) {
+            const uint32_t g = seq + t, s = g % STAGES;
+            if (!mbar_wait_bounded(smem_u32(&full[s]), (g / STAGES) & 1u) && lane == 0) {
                 atomicOr(dev_error, kErrFullWaitTimeout);
                 *s_abort = 1;
             }
             consumer_sync<WARPS * 32>();  // every warp leaves together on a timeout
-            if (*s_abort || stop[s]) break;
+            if (*s_abort) {
+                if (warp == 0 && lane == 0) *abort_flag = 1;
+                break;
+            }
+            if (stop[s]) {
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&empty[s]));
+                break;
+            }
             const uint32_t n = min((uint32_t)TILE, nsrc - t * TILE);
             const float4* tile = tiles + (size_t)s * TILE;
             const uint32_t* itile = idx_tiles + (size_t)s * TILE;
@@ -546,12 +631,19 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
         }
     } else {
         for (uint32_t t = 0; t < ntiles; ++t) {
-            const uint32_t s = t % STAGES;
-            if (!mbar_wait_bounded(smem_u32(&full[s]), (t / STAGES) & 1u)) {
-                if (lane == 0) atomicOr(dev_error, kErrFullWaitTimeout);
+            const uint32_t g = seq + t, s = g % STAGES;
+            if (!mbar_wait_bounded(smem_u32(&full[s]), (g / STAGES) & 1u)) {
+                if (lane == 0) {
+                    atomicOr(dev_error, kErrFullWaitTimeout);
+                    *abort_flag = 1;
+                }
                 break;
             }
-            if (stop[s]) break;
+            if (stop[s]) {
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&empty[s]));
+                break;
+            }
             if (!done) {
                 const uint32_t base = t * TILE;
                 const uint32_t n = min((uint32_t)TILE, nsrc - base);
@@ -585,10 +677,57 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
         }
     }
     consumer_sync<WARPS * 32>();
-    if (threadIdx.x == 0) {  // this CTA's group is group blockIdx.x
+    if (threadIdx.x == 0) {
         uint32_t sum = 0;
         for (int q = 0; q < WARPS; ++q) sum += s_gsum[q];
-        v.group_sums[blockIdx.x] = sum;
+        v.group_sums[group] = sum;
+    }
+}
+
+// One view: CTA b culls group b.
+template <int K, int WARPS, int TILE, int STAGES, bool kBinned>
+__global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v, uint32_t* __restrict__ dev_error)
+{
+    static_assert(TILE % 32 == 0, "tiles hold whole warps of lights");
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint32_t s_used, s_abort;
+    CullSmem<K, WARPS, TILE, STAGES, kBinned> sm(smem);
+    sm.init();
+    if (threadIdx.x == 0) {
+        *sm.done_warps = 0;
+        s_abort = 0;
+    }
+    __syncthreads();
+    cull_group<K, WARPS, TILE, STAGES, kBinned>(v, blockIdx.x, sm, 0, &s_used, &s_abort, dev_error);
+}
+
+// Many views in one persistent launch: each CTA takes (view, group) items from
+// `items` in queue order (an atomic counter the light-transform launch resets)
+// until none are left.  Items are ordered by decreasing expected work, so the
+// longest ones start first.
+template <int K, int WARPS, int TILE, int STAGES, bool kBinned>
+__global__ void __launch_bounds__((WARPS + 1) * 32)
+    cull_batch_kernel(const ViewJob* __restrict__ jobs, const uint2* __restrict__ items, uint32_t n_items,
+                      uint32_t* __restrict__ queue, uint32_t* __restrict__ dev_error)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint32_t s_item, s_used, s_abort;
+    CullSmem<K, WARPS, TILE, STAGES, kBinned> sm(smem);
+    sm.init();
+    if (threadIdx.x == 0) s_abort = 0;
+    uint32_t seq = 0;
+    for (;;) {
+        if (threadIdx.x == 0) {  // s_used is written by the producer before the barrier below
+            s_item = atomicAdd(queue, 1u);
+            *sm.done_warps = 0;
+        }
+        __syncthreads();
+        const uint32_t it = s_item;
+        if (it >= n_items || s_abort) break;
+        const uint2 item = items[it];
+        cull_group<K, WARPS, TILE, STAGES, kBinned>(jobs[item.x].v, item.y, sm, seq, &s_used, &s_abort, dev_error);
+        __syncthreads();
+        seq += s_used;
     }
 }
 
@@ -607,13 +746,13 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
 constexpr int kBinWarps = 32;
 constexpr int kBinChunks = 4;
 
-__global__ void __launch_bounds__(kBinWarps * 32) bin_slices_kernel(const ViewCull v)
+__device__ __forceinline__ void bin_slice_body(const ViewCull& v, uint32_t k)
 {
     __shared__ float s_lo[kBinWarps], s_hi[kBinWarps];
     __shared__ uint32_t s_cnt[kBinWarps];
     __shared__ int s_nan, s_nonfinite;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t k = blockIdx.x, xy = v.slice_clusters;
+    const uint32_t xy = v.slice_clusters;
     const float inf = __uint_as_float(0x7f800000u);
 
     float lo = inf, hi = -inf;
@@ -702,6 +841,20 @@ __global__ void __launch_bounds__(kBinWarps * 32) bin_slices_kernel(const ViewCu
     }
 }
 
+__global__ void __launch_bounds__(kBinWarps * 32) bin_slices_kernel(const ViewCull v)
+{
+    bin_slice_body(v, blockIdx.x);
+}
+
+// Batched binning: block b is slice b - prefix[v] of view v.
+__global__ void __launch_bounds__(kBinWarps * 32) batch_bin_kernel(const ViewJob* __restrict__ jobs,
+                                                                   const uint32_t* __restrict__ prefix,
+                                                                   uint32_t n_views)
+{
+    const uint32_t vi = find_view(prefix, n_views, blockIdx.x);
+    bin_slice_body(jobs[vi].v, blockIdx.x - __ldg(&prefix[vi]));
+}
+
 // ---------------------------------------------------------------------------
 // Finalize: cells = exclusive scan of counts in cluster order, packed copy.
 // ---------------------------------------------------------------------------
@@ -711,7 +864,7 @@ __global__ void __launch_bounds__(kBinWarps * 32) bin_slices_kernel(const ViewCu
 // them, warp 0 scans the 32 warp sums, pass 2 scans each row with shuffles
 // and writes the LightCells.  O(C) work and no dependency between CTAs.
 constexpr uint32_t kScanThreads = 1024;
-__global__ void __launch_bounds__(kScanThreads) scan_kernel(const ViewCull v)
+__device__ __forceinline__ void scan_body(const ViewCull& v)
 {
     constexpr uint32_t NW = kScanThreads / 32;
     constexpr int R = 8;  // rows of 32 groups each warp holds in registers per pass
@@ -759,9 +912,20 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(const ViewCull v)
 // and a warp sum), then its staging slice is copied (at most cap / 32
 // coalesced iterations).  Every warp's loads are independent of the others'.
 constexpr uint32_t kCopyWarps = 8;
-__global__ void __launch_bounds__(kCopyWarps * 32) copy_kernel(const ViewCull v)
+__global__ void __launch_bounds__(kScanThreads) scan_kernel(const ViewCull v)
 {
-    const uint32_t c = blockIdx.x * kCopyWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    scan_body(v);
+}
+
+// Batched offset scan: one CTA per view.
+__global__ void __launch_bounds__(kScanThreads) batch_scan_kernel(const ViewJob* __restrict__ jobs)
+{
+    scan_body(jobs[blockIdx.x].v);
+}
+
+__device__ __forceinline__ void copy_body(const ViewCull& v, uint32_t blk)
+{
+    const uint32_t c = blk * kCopyWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (c >= v.clusters) return;
     uint32_t b, first;
     if (v.binned) {
@@ -782,24 +946,31 @@ __global__ void __launch_bounds__(kCopyWarps * 32) copy_kernel(const ViewCull v)
     for (uint32_t i = lane; i < n; i += 32) v.indices[offset + i] = src[i];
 }
 
+__global__ void __launch_bounds__(kCopyWarps * 32) copy_kernel(const ViewCull v)
+{
+    copy_body(v, blockIdx.x);
+}
+
+// Batched copy: block b is copy block b - prefix[v] of view v.
+__global__ void __launch_bounds__(kCopyWarps * 32) batch_copy_kernel(const ViewJob* __restrict__ jobs,
+                                                                     const uint32_t* __restrict__ prefix,
+                                                                     uint32_t n_views)
+{
+    const uint32_t vi = find_view(prefix, n_views, blockIdx.x);
+    copy_body(jobs[vi].v, blockIdx.x - __ldg(&prefix[vi]));
+}
+
 template <int K, int WARPS, int TILE, int STAGES, bool kBinned>
 cudaError_t launch_cull_t(const ViewCull& v, uint32_t* dev_error, cudaStream_t stream)
 {
-    const size_t extra = kBinned ? 16 + (size_t)TILE * (sizeof(float4) + sizeof(uint32_t)) + (TILE / 32) * 4 +
-                                       (size_t)WARPS * 8 * sizeof(float) + sizeof(uint32_t)
-                                 : 0;
-    const size_t smem = (size_t)STAGES * TILE * (sizeof(float4) + (kBinned ? sizeof(uint32_t) : 0)) +
-                        2 * STAGES * sizeof(uint64_t) + (STAGES + 1) * sizeof(uint32_t) + extra;
+    static_assert(WARPS * K <= 32, "a cluster group fits one warp of the copy kernel");
+    const size_t smem = CullSmem<K, WARPS, TILE, STAGES, kBinned>::bytes();
     if (smem > 48 * 1024) {  // opt in above the default 48 KB (a per-device attribute)
         const cudaError_t e = cudaFuncSetAttribute(cull_kernel<K, WARPS, TILE, STAGES, kBinned>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    static_assert(WARPS * K <= 32, "a cluster group fits one warp of the copy kernel");
-    const uint32_t per_cta = (uint32_t)(WARPS * K);
-    const uint32_t grid = kBinned ? v.slices * ((v.slice_clusters + per_cta - 1) / per_cta)
-                                  : (v.clusters + per_cta - 1) / per_cta;
-    cull_kernel<K, WARPS, TILE, STAGES, kBinned><<<grid, (WARPS + 1) * 32, smem, stream>>>(v, dev_error);
+    cull_kernel<K, WARPS, TILE, STAGES, kBinned><<<v.groups, (WARPS + 1) * 32, smem, stream>>>(v, dev_error);
     return cudaGetLastError();
 }
 
@@ -818,7 +989,13 @@ cudaError_t launch_cull_t(const ViewCull& v, uint32_t* dev_error, cudaStream_t s
     X(4, 4, 256, 4, true)   \
     X(1, 8, 256, 4, true)   \
     X(2, 8, 256, 4, true)   \
-    X(4, 8, 256, 4, true)
+    X(4, 8, 256, 4, true)   \
+    X(1, 4, 128, 4, true)   \
+    X(2, 4, 128, 4, true)   \
+    X(4, 4, 128, 4, true)   \
+    X(1, 8, 128, 4, true)   \
+    X(2, 8, 128, 4, true)   \
+    X(4, 8, 128, 4, true)
 
 bool cull_config_supported(const CullConfig& c)
 {
@@ -919,5 +1096,98 @@ cudaError_t launch_finalize(const ViewCull& v, cudaStream_t stream)
     copy_kernel<<<(v.clusters + kCopyWarps - 1) / kCopyWarps, kCopyWarps * 32, 0, stream>>>(v);
     return cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------
+// Batches.
+// ---------------------------------------------------------------------------
+namespace {
+
+template <int K, int WARPS, int TILE, int STAGES, bool kBinned>
+cudaError_t launch_cull_batch_t(const BatchCull& b, int ctas, uint32_t* dev_error, cudaStream_t stream)
+{
+    static_assert(WARPS * K <= 32, "a cluster group fits one warp of the copy kernel");
+    const size_t smem = CullSmem<K, WARPS, TILE, STAGES, kBinned>::bytes();
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(cull_batch_kernel<K, WARPS, TILE, STAGES, kBinned>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    cull_batch_kernel<K, WARPS, TILE, STAGES, kBinned>
+        <<<ctas, (WARPS + 1) * 32, smem, stream>>>(b.jobs, b.items, b.n_items, b.queue, dev_error);
+    return cudaGetLastError();
+}
+
+template <int K, int WARPS, int TILE, int STAGES, bool kBinned>
+cudaError_t batch_occupancy_t(int* blocks)
+{
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, cull_batch_kernel<K, WARPS, TILE, STAGES, kBinned>,
+                                                         (WARPS + 1) * 32,
+                                                         CullSmem<K, WARPS, TILE, STAGES, kBinned>::bytes());
+}
+
+}  // namespace
+
+cudaError_t launch_batch_xform(const ViewJob* jobs, const uint32_t* prefix, uint32_t n_views, uint32_t blocks,
+                               uint32_t* queues, uint32_t n_queues, cudaStream_t stream)
+{
+    if (blocks == 0) {  // no lights anywhere: only the queues need resetting
+        return n_queues ? cudaMemsetAsync(queues, 0, n_queues * sizeof(uint32_t), stream) : cudaSuccess;
+    }
+    batch_xform_kernel<<<blocks, kFlagGranule, 0, stream>>>(jobs, prefix, n_views, queues, n_queues);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_bin(const ViewJob* jobs, const uint32_t* prefix, uint32_t n_views, uint32_t blocks,
+                             cudaStream_t stream)
+{
+    if (blocks == 0) return cudaSuccess;
+    batch_bin_kernel<<<blocks, kBinWarps * 32, 0, stream>>>(jobs, prefix, n_views);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_cull(const BatchCull& b, const CullConfig& cfg, int ctas, uint32_t* dev_error,
+                              cudaStream_t stream)
+{
+    if (b.n_items == 0 || ctas <= 0) return cudaSuccess;
+#define CF_DISPATCH(K, W, T, S, B)                                                                              \
+    if (cfg.clusters_per_warp == K && cfg.warps == W && cfg.tile == T && cfg.stages == S && (cfg.binned != 0) == B) \
+        return launch_cull_batch_t<K, W, T, S, B>(b, ctas, dev_error, stream);
+    CF_CULL_CONFIGS(CF_DISPATCH)
+#undef CF_DISPATCH
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t batch_cull_resident_ctas(const CullConfig& cfg, int* ctas)
+{
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+#define CF_OCC(K, W, T, S, B)                                                                                   \
+    if (cfg.clusters_per_warp == K && cfg.warps == W && cfg.tile == T && cfg.stages == S && (cfg.binned != 0) == B) \
+        e = batch_occupancy_t<K, W, T, S, B>(&per_sm);
+    CF_CULL_CONFIGS(CF_OCC)
+#undef CF_OCC
+    if (e != cudaSuccess) return e;
+    *ctas = sms * (per_sm > 0 ? per_sm : 1);
+    return cudaSuccess;
+}
+
+cudaError_t launch_batch_scan(const ViewJob* jobs, uint32_t n_views, cudaStream_t stream)
+{
+    if (n_views == 0) return cudaSuccess;
+    batch_scan_kernel<<<n_views, kScanThreads, 0, stream>>>(jobs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_copy(const ViewJob* jobs, const uint32_t* prefix, uint32_t n_views, uint32_t blocks,
+                              cudaStream_t stream)
+{
+    if (blocks == 0) return cudaSuccess;
+    batch_copy_kernel<<<blocks, kCopyWarps * 32, 0, stream>>>(jobs, prefix, n_views);
+    return cudaGetLastError();
+}
+
+uint32_t copy_blocks(uint32_t clusters) { return (clusters + kCopyWarps - 1) / kCopyWarps; }
 
 }  // namespace cfk

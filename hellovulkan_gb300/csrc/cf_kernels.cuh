@@ -68,6 +68,16 @@ struct ViewCull {
     uint32_t binned;
 };
 
+// One view of a batch: its culling state plus the inputs of the per-view
+// stages, and where its blocks start in each batched launch.
+struct ViewJob {
+    ViewCull v;
+    const CfLightData* lights;
+    uint32_t light_count;
+    uint32_t pad_[3];
+    float view[16];  // cameraView, column-major
+};
+
 // First cluster and end of group b (see ViewCull).
 __host__ __device__ inline void group_range(const ViewCull& v, uint32_t b, uint32_t* first, uint32_t* end)
 {
@@ -117,5 +127,27 @@ cudaError_t launch_light_xform(const CfLightData* lights, uint32_t count, const 
 cudaError_t launch_bin(const ViewCull& v, cudaStream_t stream);
 cudaError_t launch_cull(const ViewCull& v, const CullConfig& cfg, uint32_t* dev_error, cudaStream_t stream);
 cudaError_t launch_finalize(const ViewCull& v, cudaStream_t stream);
+
+// Batches: every stage of many views in one launch (the culling stage once per
+// shape bucket).  `prefix` arrays hold, per view, the first block of that view
+// in the launch; `blocks` is the launch's total.
+struct BatchCull {
+    const ViewJob* jobs;
+    const uint2* items;  // (view, group) in the order the queue hands them out
+    uint32_t n_items;
+    uint32_t* queue;     // reset to 0 by launch_batch_xform
+};
+constexpr uint32_t kMaxBatchQueues = 256;  // queues a batch_xform launch resets (<= its block size)
+cudaError_t launch_batch_xform(const ViewJob* jobs, const uint32_t* prefix, uint32_t n_views, uint32_t blocks,
+                               uint32_t* queues, uint32_t n_queues, cudaStream_t stream);
+cudaError_t launch_batch_bin(const ViewJob* jobs, const uint32_t* prefix, uint32_t n_views, uint32_t blocks,
+                             cudaStream_t stream);
+cudaError_t launch_batch_cull(const BatchCull& b, const CullConfig& cfg, int ctas, uint32_t* dev_error,
+                              cudaStream_t stream);
+cudaError_t batch_cull_resident_ctas(const CullConfig& cfg, int* ctas);
+cudaError_t launch_batch_scan(const ViewJob* jobs, uint32_t n_views, cudaStream_t stream);
+cudaError_t launch_batch_copy(const ViewJob* jobs, const uint32_t* prefix, uint32_t n_views, uint32_t blocks,
+                              cudaStream_t stream);
+uint32_t copy_blocks(uint32_t clusters);
 
 }  // namespace cfk

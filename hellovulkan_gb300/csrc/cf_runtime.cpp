@@ -17,6 +17,7 @@
 #include <new>
 #include <string>
 
+#include "cf_batch_internal.h"
 #include "cf_kernels.cuh"
 #include "cf_runtime_internal.h"
 #include "cfcull.h"
@@ -221,6 +222,11 @@ struct CfPipelineLightCulling {
     cudaEvent_t stage_events[4] = {nullptr, nullptr, nullptr, nullptr};  // stage timing, when enabled
     unsigned long long* d_work = nullptr;                                   // work counters, when enabled
 };
+
+namespace cfrt {
+int context_device(const CfContext* ctx) { return ctx->device; }
+uint32_t* context_error_word(const CfContext* ctx) { return ctx->dev_error; }
+}  // namespace cfrt
 
 namespace {
 

@@ -196,6 +196,61 @@ CFCULL_API int cf_pipeline_light_culling_enable_work_counters(CfPipelineLightCul
 CFCULL_API int cf_pipeline_light_culling_read_work_counters(CfPipelineLightCulling* pipe, uint64_t counters[2]);
 
 /* ------------------------------------------------------------------------ */
+/* Batches: many views culled together.  No counterpart in the reference,     */
+/* which culls one view per frame; each view's outputs are the ones           */
+/* PipelineLightCulling would produce for it.                                 */
+/* ------------------------------------------------------------------------ */
+typedef struct CfBatch CfBatch;
+
+/* One view of a batch; every pointer is caller-owned device memory that must
+ * stay valid while the batch uses it. */
+typedef struct CfBatchView {
+    CfClusterForwardUBO ubo;        /* grid, projection and view of this view     */
+    const CfLightData* d_lights;    /* light_count records                        */
+    CfAABB* d_aabbs;                /* X*Y*Z boxes (written by generate_aabbs)    */
+    CfLightCell* d_cells;           /* X*Y*Z cells (output)                       */
+    uint32_t* d_indices;            /* index list (output)                        */
+    uint32_t* d_total;              /* optional: indices written (output)         */
+    uint64_t index_capacity;        /* >= X*Y*Z * max_lights_per_cluster          */
+    uint32_t light_count;
+    uint32_t max_lights_per_cluster;
+    uint32_t _pad[2];
+} CfBatchView;
+
+typedef struct CfBatchInfo {
+    uint32_t views, items, buckets, _pad;
+    uint64_t workspace_bytes;
+    uint32_t bucket_slice_clusters[8]; /* first 8 buckets: X*Y of their views      */
+    int32_t bucket_config[8][4];       /* clusters/warp, warps, tile, stages        */
+    int32_t bucket_ctas[8];            /* persistent CTAs of their culling launch   */
+} CfBatchInfo;
+
+CFCULL_API int cf_batch_create(CfContext* ctx, CfBatch** out);
+CFCULL_API int cf_batch_destroy(CfBatch* batch);
+/* Replaces the batch's views (copied); allocates its workspace and builds its
+ * work-item tables.  Synchronous. */
+CFCULL_API int cf_batch_set_views(CfBatch* batch, const CfBatchView* views, uint32_t count);
+/* Updates the view matrices (cameraView of each UBO; the projection part must
+ * not change) for the next cf_batch_cull.  Synchronises `stream`. */
+CFCULL_API int cf_batch_update_view_matrices(CfBatch* batch, const CfClusterForwardUBO* ubos, uint32_t count,
+                                             void* stream);
+/* AABBGenerator.comp for every view into its d_aabbs. */
+CFCULL_API int cf_batch_generate_aabbs(CfBatch* batch, void* stream);
+/* One culling pass over every view.  With graphs enabled (the default) and a
+ * non-null stream, the first call captures the pass into a CUDA graph and
+ * later calls replay it. */
+CFCULL_API int cf_batch_cull(CfBatch* batch, void* stream);
+CFCULL_API int cf_batch_set_graph(CfBatch* batch, int enable);
+/* Fixes the culling configuration of the views whose grid has slice_clusters
+ * = X*Y clusters per depth slice (clusters_per_warp 0 = default). */
+CFCULL_API int cf_batch_set_tuning(CfBatch* batch, uint32_t slice_clusters, int clusters_per_warp, int warps,
+                                   int tile, int stages);
+/* Times every candidate configuration on the current views, `repeats` passes
+ * each, and keeps the fastest per shape bucket (views sharing X*Y). */
+CFCULL_API int cf_batch_autotune(CfBatch* batch, int repeats, void* stream);
+CFCULL_API int cf_batch_get_info(const CfBatch* batch, CfBatchInfo* info);
+
+/* ------------------------------------------------------------------------ */
 /* Stateless entry points on caller-owned device memory.                     */
 /* ------------------------------------------------------------------------ */
 

@@ -82,6 +82,52 @@ class CfBatchInfo(C.Structure):
     ]
 
 
+class CfServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_batch_views", C.c_uint32), ("streams", C.c_uint32),
+                ("max_pending", C.c_uint32), ("max_groups_per_view", C.c_uint32)]
+
+
+class CfServerRequest(C.Structure):
+    _fields_ = [("ubo", CfClusterForwardUBO), ("light_set", C.c_uint64), ("user_tag", C.c_uint64),
+                ("max_lights_per_cluster", C.c_uint32), ("_pad", C.c_uint32 * 3)]
+
+
+class CfServerCompletion(C.Structure):
+    _fields_ = [("request_id", C.c_uint64), ("user_tag", C.c_uint64), ("status", C.c_int32),
+                ("clusters", C.c_uint32), ("t_submit", C.c_double), ("t_launch", C.c_double),
+                ("t_complete", C.c_double), ("d_cells", C.c_void_p), ("d_indices", C.c_void_p),
+                ("d_total", C.c_void_p)]
+
+
+class CfServerStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("submitted", "completed", "batches", "views_launched", "max_pending",
+                                          "evictions", "arena_bytes", "arena_used_bytes", "arena_peak_bytes",
+                                          "pending", "resident_light_sets", "resident_projections")] + [
+        ("max_batch_views", C.c_uint32), ("_pad", C.c_uint32)]
+
+
+class CfServeLoad(C.Structure):
+    _fields_ = [("rate_per_s", C.c_double), ("duration_s", C.c_double), ("p_reuse", C.c_double),
+                ("seed", C.c_uint64), ("jitter_sigma", C.c_float), ("recent_sets", C.c_uint32),
+                ("submit_threads", C.c_uint32), ("max_lights_per_cluster", C.c_uint32),
+                ("n_projections", C.c_uint32), ("n_base_sets", C.c_uint32),
+                ("projections", C.c_void_p), ("base_sets", C.c_void_p), ("base_counts", C.c_void_p),
+                ("eye_lo", C.c_float * 3), ("eye_hi", C.c_float * 3), ("target_lo", C.c_float * 3),
+                ("target_hi", C.c_float * 3)]
+
+
+class CfServeReport(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("scheduled", "submitted", "completed", "failed", "new_sets",
+                                          "reused_sets", "tests_brute_force")] + [
+        (n, C.c_double) for n in ("wall_s", "offered_rate", "achieved_rate", "latency_p50_ms", "latency_p90_ms",
+                                  "latency_p99_ms", "latency_p999_ms", "latency_max_ms", "queue_p50_ms",
+                                  "queue_p99_ms", "submit_lag_p99_ms")]
+
+
+assert C.sizeof(CfServerConfig) == 24 and C.sizeof(CfServerRequest) == 208
+assert C.sizeof(CfServerCompletion) == 72 and C.sizeof(CfServerStats) == 104
+assert C.sizeof(CfServeLoad) == 128 and C.sizeof(CfServeReport) == 144
+assert CfServeLoad.projections.offset == 56 and CfServeLoad.eye_lo.offset == 80
 assert C.sizeof(CfBatchView) == 240 and C.sizeof(CfBatchInfo) == 216
 assert C.sizeof(CfLightData) == 48 and C.sizeof(CfAABB) == 32 and C.sizeof(CfLightCell) == 8
 assert C.sizeof(CfClusterForwardUBO) == 176
@@ -157,6 +203,19 @@ _SIGS = {
     "cf_batch_set_tuning": [_P, _U32, _I, _I, _I, _I],
     "cf_batch_autotune": [_P, _I, _P],
     "cf_batch_get_info": [_P, C.POINTER(CfBatchInfo)],
+    "cf_server_create": [_P, C.POINTER(CfServerConfig), C.POINTER(_P)],
+    "cf_server_destroy": [_P],
+    "cf_server_register_light_set": [_P, _P, _U32, _PU64],
+    "cf_server_update_light_set": [_P, _U64, _P, _U32],
+    "cf_server_jitter_light_set": [_P, _U64, _U64, C.c_float],
+    "cf_server_release_light_set": [_P, _U64],
+    "cf_server_is_light_set_resident": [_P, _U64, C.POINTER(_I)],
+    "cf_server_submit": [_P, C.POINTER(CfServerRequest), _PU64],
+    "cf_server_poll": [_P, C.POINTER(CfServerCompletion), _U32, _PU32, _I],
+    "cf_server_release": [_P, _U64],
+    "cf_server_set_tuning": [_P, _U32, _I, _I, _I, _I],
+    "cf_server_get_stats": [_P, C.POINTER(CfServerStats)],
+    "cf_serve_run_load": [_P, C.POINTER(CfServeLoad), C.POINTER(CfServeReport)],
 }
 _RESTYPE = {"cf_status_string": C.c_char_p, "cf_last_error_message": C.c_char_p}
 

@@ -1098,6 +1098,55 @@ cudaError_t launch_finalize(const ViewCull& v, cudaStream_t stream)
 }
 
 // ---------------------------------------------------------------------------
+// Light jitter: dst = src with every position coordinate moved by sigma times
+// an Irwin-Hall variate (the sum of 12 uniforms in [0, 1) minus 6, mean 0,
+// variance 1, a close stand-in for a unit Gaussian).  The uniforms come from
+// a splitmix64 finaliser over (seed, light, axis, term), so the host can
+// reproduce every bit: u = (hash >> 40) * 2^-24, summed in term order with
+// round-to-nearest adds, then scaled and added with one rounding each.
+// ---------------------------------------------------------------------------
+namespace {
+
+__device__ __forceinline__ uint64_t splitmix_finalise(uint64_t x)
+{
+    x ^= x >> 30;
+    x *= 0xBF58476D1CE4E5B9ull;
+    x ^= x >> 27;
+    x *= 0x94D049BB133111EBull;
+    x ^= x >> 31;
+    return x;
+}
+
+__global__ void __launch_bounds__(256) jitter_kernel(const CfLightData* __restrict__ src, CfLightData* __restrict__ dst,
+                                                     uint32_t n, uint64_t seed, float sigma)
+{
+    const uint32_t i = blockIdx.x * 256 + threadIdx.x;
+    if (i >= n) return;
+    CfLightData L = src[i];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float s = 0.0f;
+        for (int k = 0; k < 12; ++k) {
+            const uint64_t h = splitmix_finalise(seed + (uint64_t)i * 0x9E3779B97F4A7C15ull +
+                                                 (uint64_t)(a * 12 + k) * 0xD1B54A32D192ED03ull);
+            s = __fadd_rn(s, __fmul_rn((float)(uint32_t)(h >> 40), 0x1p-24f));
+        }
+        L.position[a] = __fadd_rn(L.position[a], __fmul_rn(sigma, __fsub_rn(s, 6.0f)));
+    }
+    dst[i] = L;
+}
+
+}  // namespace
+
+cudaError_t launch_jitter(const CfLightData* src, CfLightData* dst, uint32_t n, uint64_t seed, float sigma,
+                          cudaStream_t stream)
+{
+    if (n == 0) return cudaSuccess;
+    jitter_kernel<<<(n + 255) / 256, 256, 0, stream>>>(src, dst, n, seed, sigma);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Batches.
 // ---------------------------------------------------------------------------
 namespace {

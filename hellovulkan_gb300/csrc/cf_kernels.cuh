@@ -127,6 +127,9 @@ cudaError_t launch_light_xform(const CfLightData* lights, uint32_t count, const 
 cudaError_t launch_bin(const ViewCull& v, cudaStream_t stream);
 cudaError_t launch_cull(const ViewCull& v, const CullConfig& cfg, uint32_t* dev_error, cudaStream_t stream);
 cudaError_t launch_finalize(const ViewCull& v, cudaStream_t stream);
+// dst = src with positions moved by sigma * (Irwin-Hall variate) from (seed, light, axis).
+cudaError_t launch_jitter(const CfLightData* src, CfLightData* dst, uint32_t n, uint64_t seed, float sigma,
+                          cudaStream_t stream);
 
 // Batches: every stage of many views in one launch (the culling stage once per
 // shape bucket).  `prefix` arrays hold, per view, the first block of that view

@@ -1,0 +1,904 @@
+// cf_server.cpp — a culling server with continuous batching.
+//
+// Requests (a view's UBO + the id of a light set resident on the device) are
+// submitted from any thread and admitted in arrival order by one worker
+// thread.  Admission takes device memory for the request's scratch and
+// outputs from one arena whose size is the server's HBM budget; light sets
+// and the AABBs of each distinct projection live in the same arena and are
+// evicted least-recently-used when admission needs room (never while a
+// request in flight uses them).  Whenever one of the server's streams is
+// free, every admissible pending request (up to max_batch_views) is launched
+// there as one batch — so requests that arrive while earlier batches are
+// still on the GPU start on another stream and overlap with them.  A host
+// callback on the stream timestamps the batch's completion.
+//
+// Light-set updates are copy-on-write: requests already admitted keep the
+// version they were admitted with, so a result never depends on what else is
+// in flight.  The same request gives the same bits alone and in any mix.
+//
+// The reference has no counterpart (its one view per frame is recorded by
+// AppBase::DrawFrame, Source/Apps/AppBase.cpp:94-196).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "cf_arena.h"
+#include "cf_batch_internal.h"
+#include "cf_kernels.cuh"
+#include "cf_runtime_internal.h"
+#include "cfcull.h"
+
+using namespace cfrt;
+
+namespace {
+
+double now_s()
+{
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct LightVersion {
+    unsigned char* d = nullptr;
+    uint32_t count = 0;
+    uint32_t refs = 0;
+    bool retired = false;
+    cudaEvent_t ready = nullptr;      // the upload (or jitter) that fills it
+    cudaEvent_t last_read = nullptr;  // the last jitter that reads it, if any
+};
+
+struct LightSet {
+    LightVersion* cur = nullptr;
+    uint64_t last_use = 0;
+};
+
+struct AabbEntry {
+    CfClusterForwardUBO key{};
+    unsigned char* d = nullptr;
+    uint32_t refs = 0;
+    bool generated = false;
+    cudaEvent_t ready = nullptr;
+    uint64_t last_use = 0;
+};
+
+struct Request {
+    uint64_t id = 0;
+    CfServerRequest req{};
+    double t_submit = 0, t_launch = 0, t_complete = 0;
+    LightVersion* lights = nullptr;
+    AabbEntry* aabb = nullptr;
+    unsigned char* ws = nullptr;
+    unsigned char* out = nullptr;
+    uint32_t clusters = 0;
+    cfk::CullConfig cfg{};
+    cfk::WorkspaceLayout layout{};
+    int status = CF_SUCCESS;
+};
+
+struct Batch;
+
+struct StreamSlot {
+    cudaStream_t s = nullptr;
+    bool busy = false;
+    cfk::ViewJob* d_jobs = nullptr;
+    uint32_t* d_prefix = nullptr;
+    uint2* d_items = nullptr;
+    uint32_t* d_queues = nullptr;
+    cfk::ViewJob* h_jobs = nullptr;
+    uint32_t* h_prefix = nullptr;
+    uint2* h_items = nullptr;
+};
+
+struct Batch {
+    CfServer* server = nullptr;
+    int slot = 0;
+    std::vector<Request*> reqs;
+    double t_done = 0;
+};
+
+size_t output_bytes(uint32_t clusters, uint32_t cap)
+{
+    const size_t cells = ((size_t)clusters * sizeof(CfLightCell) + 255) & ~(size_t)255;
+    const size_t idx = ((size_t)clusters * cap * sizeof(uint32_t) + 255) & ~(size_t)255;
+    return cells + idx + 256;
+}
+
+void out_pointers(unsigned char* out, uint32_t clusters, uint32_t cap, CfLightCell** cells, uint32_t** idx,
+                  uint32_t** total)
+{
+    const size_t cb = ((size_t)clusters * sizeof(CfLightCell) + 255) & ~(size_t)255;
+    const size_t ib = ((size_t)clusters * cap * sizeof(uint32_t) + 255) & ~(size_t)255;
+    *cells = reinterpret_cast<CfLightCell*>(out);
+    *idx = reinterpret_cast<uint32_t*>(out + cb);
+    *total = reinterpret_cast<uint32_t*>(out + cb + ib);
+}
+
+}  // namespace
+
+struct CfServer {
+    CfContext* ctx = nullptr;
+    int device = 0;
+    uint32_t* dev_error = nullptr;
+    CfServerConfig cfg{};
+    unsigned char* d_pool = nullptr;
+    Arena arena;
+    std::mutex mu;
+    std::condition_variable cv, done_cv;
+    std::deque<Request*> pending;
+    std::vector<StreamSlot> slots;
+    std::map<uint64_t, LightSet> sets;
+    std::vector<AabbEntry*> aabbs;
+    std::map<uint64_t, Request*> holding;  // completed, outputs not yet released
+    std::deque<CfServerCompletion> completions;
+    // Finished batches, handed over by the stream host callback.  The callback
+    // takes only done_mu (never `mu`), so no thread holding `mu` can ever wait
+    // on a callback that waits on it.
+    std::mutex done_mu;
+    std::deque<Batch*> finished;
+    std::atomic<uint32_t> finished_n{0};
+    std::map<uint32_t, cfk::CullConfig> tuned;
+    std::vector<std::pair<unsigned char*, cudaEvent_t>> deferred;  // freed once the event has completed
+    std::thread worker;
+    bool stop = false;
+    cudaStream_t upload = nullptr;
+    uint64_t next_set = 1, next_req = 1, tick = 0;
+    uint64_t memory_epoch = 0;  // bumped whenever device memory returns to the arena
+    uint32_t items_per_slot = 0;
+    CfServerStats stats{};
+    double t0 = 0;
+};
+
+namespace {
+
+cfk::CullConfig server_config_for(const CfServer* s, uint32_t xy)
+{
+    auto it = s->tuned.find(xy);
+    if (it != s->tuned.end()) return it->second;
+    return xy <= 64 ? cfk::CullConfig{2, 4, 256, 4, 1} : cfk::CullConfig{4, 4, 256, 4, 1};
+}
+
+void free_version_if_dead(CfServer* s, LightVersion* v)
+{
+    if (v && v->retired && v->refs == 0) {
+        if (v->last_read) s->deferred.emplace_back(v->d, v->last_read);  // a jitter may still read it
+        else s->arena.release(v->d);
+        if (v->ready) cudaEventDestroy(v->ready);
+        delete v;
+    }
+}
+
+void reap_deferred(CfServer* s)
+{
+    auto keep = s->deferred.begin();
+    for (auto it = s->deferred.begin(); it != s->deferred.end(); ++it) {
+        if (cudaEventQuery(it->second) == cudaSuccess) {
+            s->arena.release(it->first);
+            cudaEventDestroy(it->second);
+        } else {
+            *keep++ = *it;
+        }
+    }
+    s->deferred.erase(keep, s->deferred.end());
+}
+
+// Frees the least recently used light set or AABB entry nobody in flight
+// uses; false when there is none.
+bool evict_one(CfServer* s)
+{
+    uint64_t best = UINT64_MAX;
+    int kind = -1;
+    uint64_t set_id = 0;
+    size_t aabb_i = 0;
+    for (auto& kv : s->sets)
+        if (kv.second.cur->refs == 0 && kv.second.last_use < best) {
+            best = kv.second.last_use;
+            kind = 0;
+            set_id = kv.first;
+        }
+    for (size_t i = 0; i < s->aabbs.size(); ++i)
+        if (s->aabbs[i]->refs == 0 && s->aabbs[i]->last_use < best) {
+            best = s->aabbs[i]->last_use;
+            kind = 1;
+            aabb_i = i;
+        }
+    if (kind == 0) {
+        LightVersion* v = s->sets[set_id].cur;
+        v->retired = true;
+        free_version_if_dead(s, v);
+        s->sets.erase(set_id);
+        s->stats.evictions++;
+        return true;
+    }
+    if (kind == 1) {
+        AabbEntry* a = s->aabbs[aabb_i];
+        s->arena.release(a->d);
+        if (a->ready) cudaEventDestroy(a->ready);
+        delete a;
+        s->aabbs.erase(s->aabbs.begin() + (long)aabb_i);
+        s->stats.evictions++;
+        return true;
+    }
+    return false;
+}
+
+unsigned char* arena_alloc(CfServer* s, size_t bytes)
+{
+    reap_deferred(s);
+    for (;;) {
+        unsigned char* p = s->arena.alloc(bytes);
+        if (p) {
+            s->stats.arena_peak_bytes = std::max<uint64_t>(s->stats.arena_peak_bytes, s->arena.used());
+            return p;
+        }
+        if (!evict_one(s)) return nullptr;
+    }
+}
+
+void complete_request(CfServer* s, Request* r, int status)
+{
+    CfServerCompletion c{};
+    c.request_id = r->id;
+    c.user_tag = r->req.user_tag;
+    c.status = status;
+    c.t_submit = r->t_submit - s->t0;
+    c.t_launch = r->t_launch ? r->t_launch - s->t0 : 0;
+    c.t_complete = r->t_complete - s->t0;
+    c.clusters = r->clusters;
+    if (status == CF_SUCCESS) {
+        CfLightCell* cells;
+        uint32_t *idx, *total;
+        out_pointers(r->out, r->clusters, r->req.max_lights_per_cluster, &cells, &idx, &total);
+        c.d_cells = cells;
+        c.d_indices = idx;
+        c.d_total = total;
+        s->holding[r->id] = r;
+    } else {
+        s->arena.release(r->out);
+        delete r;
+    }
+    s->completions.push_back(c);
+    s->stats.completed++;
+    s->done_cv.notify_all();
+}
+
+// Takes what request r needs; false (nothing taken) when the arena is full.
+bool admit(CfServer* s, Request* r)
+{
+    const CfClusterForwardUBO& u = r->req.ubo;
+    LightVersion* lv = r->lights;  // bound (and referenced) at submission
+    const uint32_t xy = u.sliceCountX * u.sliceCountY, Z = u.sliceCountZ;
+    r->cfg = server_config_for(s, xy);
+    const uint32_t groups = cfk::group_count(r->clusters, xy, Z, (uint32_t)(r->cfg.warps * r->cfg.clusters_per_warp), true);
+    if (groups > s->cfg.max_groups_per_view) {
+        r->status = CF_ERROR_CAPACITY;
+        return true;
+    }
+    r->layout = cfk::workspace_layout(r->clusters, lv->count, r->req.max_lights_per_cluster, Z, true, groups);
+    AabbEntry* a = nullptr;
+    for (AabbEntry* e : s->aabbs)
+        if (projection_equal(e->key, u)) a = e;
+    bool new_aabb = false;
+    if (a) {
+        a->refs++;  // the AABBs may not be evicted by the allocations below
+    } else {
+        a = new AabbEntry();
+        a->key = u;
+        a->d = arena_alloc(s, (size_t)r->clusters * sizeof(CfAABB));
+        if (!a->d) {
+            delete a;
+            return false;
+        }
+        a->refs = 1;
+        s->aabbs.push_back(a);
+        new_aabb = true;
+    }
+    r->ws = arena_alloc(s, r->layout.bytes);
+    r->out = r->ws ? arena_alloc(s, output_bytes(r->clusters, r->req.max_lights_per_cluster)) : nullptr;
+    if (!r->ws || !r->out) {
+        s->arena.release(r->ws);
+        r->ws = nullptr;
+        a->refs--;
+        if (new_aabb) {
+            s->arena.release(a->d);
+            s->aabbs.erase(std::find(s->aabbs.begin(), s->aabbs.end(), a));
+            delete a;
+        }
+        return false;
+    }
+    r->aabb = a;
+    auto it = s->sets.find(r->req.light_set);
+    if (it != s->sets.end()) it->second.last_use = ++s->tick;
+    a->last_use = ++s->tick;
+    return true;
+}
+
+void CUDART_CB on_batch_done(void* data)
+{
+    Batch* b = static_cast<Batch*>(data);
+    b->t_done = now_s();
+    CfServer* s = b->server;
+    {
+        std::lock_guard<std::mutex> lk(s->done_mu);
+        s->finished.push_back(b);
+    }
+    s->finished_n.fetch_add(1);
+    s->cv.notify_all();
+}
+
+// Moves the batches the callbacks finished into `out` (called with `mu` held).
+void take_finished(CfServer* s, std::deque<Batch*>& out)
+{
+    std::lock_guard<std::mutex> lk(s->done_mu);
+    out.swap(s->finished);
+    s->finished_n.fetch_sub((uint32_t)out.size());
+}
+
+int launch_batch(CfServer* s, int slot_i, std::vector<Request*>& reqs)
+{
+    StreamSlot& sl = s->slots[slot_i];
+    const uint32_t n = (uint32_t)reqs.size();
+    cudaStream_t st = sl.s;
+    cudaError_t e = cudaSuccess;
+    // inputs produced elsewhere: light uploads and AABBs generated by other batches
+    for (Request* r : reqs) {
+        if (r->lights->ready) e = cudaStreamWaitEvent(st, r->lights->ready, 0);
+        if (e != cudaSuccess) return cuda_fail(e, "wait for light upload");
+        AabbEntry* a = r->aabb;
+        if (!a->generated) {
+            e = cfk::launch_aabb(r->req.ubo, reinterpret_cast<CfAABB*>(a->d), st);
+            if (e == cudaSuccess && !a->ready) e = cudaEventCreateWithFlags(&a->ready, cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventRecord(a->ready, st);
+            if (e != cudaSuccess) return cuda_fail(e, "AABB generation");
+            a->generated = true;
+        } else if (a->ready) {
+            e = cudaStreamWaitEvent(st, a->ready, 0);
+            if (e != cudaSuccess) return cuda_fail(e, "wait for AABBs");
+        }
+    }
+    // tables
+    std::map<uint32_t, std::vector<uint32_t>> buckets;
+    uint32_t xb = 0, bb = 0, cb = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        Request* r = reqs[i];
+        const CfClusterForwardUBO& u = r->req.ubo;
+        cfk::ViewJob& j = sl.h_jobs[i];
+        j = cfk::ViewJob{};
+        const cfk::WorkspaceLayout& L = r->layout;
+        unsigned char* w = r->ws;
+        CfLightCell* cells;
+        uint32_t *idx, *total;
+        out_pointers(r->out, r->clusters, r->req.max_lights_per_cluster, &cells, &idx, &total);
+        j.v.vlights = reinterpret_cast<const float4*>(w + L.vlights);
+        j.v.nonfinite = reinterpret_cast<const uint32_t*>(w + L.nonfinite);
+        j.v.aabbs = reinterpret_cast<const float4*>(r->aabb->d);
+        j.v.counts = reinterpret_cast<uint32_t*>(w + L.counts);
+        j.v.staging = reinterpret_cast<uint32_t*>(w + L.staging);
+        j.v.cells = cells;
+        j.v.indices = idx;
+        j.v.total = total;
+        j.v.slice_lights = reinterpret_cast<float4*>(w + L.slice_lights);
+        j.v.slice_idx = reinterpret_cast<uint32_t*>(w + L.slice_idx);
+        j.v.slice_count = reinterpret_cast<uint32_t*>(w + L.slice_count);
+        j.v.slice_nonfinite = reinterpret_cast<uint32_t*>(w + L.slice_nonfinite);
+        j.v.group_sums = reinterpret_cast<uint32_t*>(w + L.group_sums);
+        j.v.group_offsets = reinterpret_cast<uint32_t*>(w + L.group_offsets);
+        j.v.lpad = cfk::pad_lights(r->lights->count);
+        j.v.clusters = r->clusters;
+        j.v.cap = r->req.max_lights_per_cluster;
+        j.v.slice_clusters = u.sliceCountX * u.sliceCountY;
+        j.v.slices = u.sliceCountZ;
+        j.v.group_width = (uint32_t)(r->cfg.warps * r->cfg.clusters_per_warp);
+        j.v.groups = cfk::group_count(r->clusters, j.v.slice_clusters, j.v.slices, j.v.group_width, true);
+        j.v.binned = 1;
+        j.lights = reinterpret_cast<const CfLightData*>(r->lights->d);
+        j.light_count = r->lights->count;
+        for (int q = 0; q < 16; ++q) j.view[q] = u.cameraView[q];
+        sl.h_prefix[i] = xb;
+        sl.h_prefix[n + i] = bb;
+        sl.h_prefix[2 * n + i] = cb;
+        xb += cfk::granules(j.v.lpad);
+        bb += j.v.slices;
+        cb += cfk::copy_blocks(r->clusters);
+        buckets[j.v.slice_clusters].push_back(i);
+    }
+    struct B {
+        cfk::CullConfig cfg;
+        uint32_t begin, count;
+    };
+    std::vector<B> bl;
+    uint32_t ni = 0;
+    for (auto& kv : buckets) {
+        B bk{reqs[kv.second[0]]->cfg, ni, 0};
+        for (uint32_t vi : kv.second)
+            for (uint32_t g = 0; g < sl.h_jobs[vi].v.groups; ++g) sl.h_items[ni++] = make_uint2(vi, g);
+        bk.count = ni - bk.begin;
+        bl.push_back(bk);
+    }
+    e = cudaMemcpyAsync(sl.d_jobs, sl.h_jobs, n * sizeof(cfk::ViewJob), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(sl.d_prefix, sl.h_prefix, 3 * n * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && ni) e = cudaMemcpyAsync(sl.d_items, sl.h_items, ni * sizeof(uint2), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cfk::launch_batch_xform(sl.d_jobs, sl.d_prefix, n, xb, sl.d_queues, (uint32_t)bl.size(), st);
+    if (e == cudaSuccess) e = cfk::launch_batch_bin(sl.d_jobs, sl.d_prefix + n, n, bb, st);
+    for (size_t q = 0; q < bl.size() && e == cudaSuccess; ++q) {
+        int ctas = 0;
+        e = cfk::batch_cull_resident_ctas(bl[q].cfg, &ctas);
+        if (e != cudaSuccess) break;
+        cfk::BatchCull bc{sl.d_jobs, sl.d_items + bl[q].begin, bl[q].count, sl.d_queues + q};
+        e = cfk::launch_batch_cull(bc, bl[q].cfg, std::min<int>(ctas, (int)bl[q].count), s->dev_error, st);
+    }
+    if (e == cudaSuccess) e = cfk::launch_batch_scan(sl.d_jobs, n, st);
+    if (e == cudaSuccess) e = cfk::launch_batch_copy(sl.d_jobs, sl.d_prefix + 2 * n, n, cb, st);
+    if (e != cudaSuccess) return cuda_fail(e, "server batch launch");
+    Batch* b = new Batch();
+    b->server = s;
+    b->slot = slot_i;
+    b->reqs = reqs;
+    const double t = now_s();
+    for (Request* r : reqs) r->t_launch = t;
+    e = cudaLaunchHostFunc(st, on_batch_done, b);
+    if (e != cudaSuccess) {
+        delete b;
+        return cuda_fail(e, "cudaLaunchHostFunc");
+    }
+    sl.busy = true;
+    s->stats.batches++;
+    s->stats.views_launched += n;
+    s->stats.max_batch_views = std::max<uint32_t>(s->stats.max_batch_views, n);
+    return CF_SUCCESS;
+}
+
+void finish_batch(CfServer* s, Batch* b)
+{
+    s->slots[b->slot].busy = false;
+    for (Request* r : b->reqs) {
+        r->t_complete = b->t_done;
+        r->lights->refs--;
+        free_version_if_dead(s, r->lights);
+        r->aabb->refs--;
+        s->arena.release(r->ws);
+        r->ws = nullptr;
+        complete_request(s, r, CF_SUCCESS);
+    }
+    delete b;
+}
+
+void worker_main(CfServer* s)
+{
+    DeviceGuard g(s->device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    uint64_t blocked_at = UINT64_MAX;  // memory epoch at which the head request did not fit
+    for (;;) {
+        std::deque<Batch*> done;
+        take_finished(s, done);
+        for (Batch* b : done) finish_batch(s, b);
+        if (!done.empty()) s->memory_epoch++;
+        if (blocked_at != s->memory_epoch) blocked_at = UINT64_MAX;
+        bool launched = false;
+        for (size_t q = 0; q < s->slots.size() && !s->pending.empty() && blocked_at == UINT64_MAX; ++q) {
+            if (s->slots[q].busy) continue;
+            std::vector<Request*> batch;
+            while (!s->pending.empty() && batch.size() < s->cfg.max_batch_views) {
+                Request* r = s->pending.front();
+                if (!admit(s, r)) {  // arena full: wait until memory is freed (arrival order is kept)
+                    blocked_at = s->memory_epoch;
+                    break;
+                }
+                s->pending.pop_front();
+                if (r->status != CF_SUCCESS) {
+                    r->lights->refs--;
+                    free_version_if_dead(s, r->lights);
+                    r->t_complete = now_s();
+                    complete_request(s, r, r->status);
+                    continue;
+                }
+                batch.push_back(r);
+            }
+            if (batch.empty()) {
+                // Nothing fits.  With nothing in flight or held there is nothing
+                // to wait for: the request alone exceeds the budget.
+                const bool inflight = std::any_of(s->slots.begin(), s->slots.end(),
+                                                  [](const StreamSlot& x) { return x.busy; });
+                if (!inflight && s->holding.empty() && !s->pending.empty()) {
+                    Request* r = s->pending.front();
+                    s->pending.pop_front();
+                    r->lights->refs--;
+                    free_version_if_dead(s, r->lights);
+                    r->t_complete = now_s();
+                    complete_request(s, r, CF_ERROR_BUDGET);
+                    blocked_at = UINT64_MAX;
+                    continue;
+                }
+                break;
+            }
+            const int st = launch_batch(s, (int)q, batch);
+            if (st != CF_SUCCESS) {
+                for (Request* r : batch) {
+                    r->lights->refs--;
+                    free_version_if_dead(s, r->lights);
+                    r->aabb->refs--;
+                    s->arena.release(r->ws);
+                    r->t_complete = now_s();
+                    complete_request(s, r, st);
+                }
+            } else {
+                launched = true;
+            }
+        }
+        const bool busy = std::any_of(s->slots.begin(), s->slots.end(), [](const StreamSlot& x) { return x.busy; });
+        if (s->stop && s->pending.empty() && !busy && s->finished_n.load() == 0) break;
+        if (!launched)
+            s->cv.wait_for(lk, std::chrono::milliseconds(2), [s, blocked_at] {
+                if (s->stop || s->finished_n.load() > 0) return true;
+                if (blocked_at != UINT64_MAX) return s->memory_epoch != blocked_at;  // wait for freed memory
+                return !s->pending.empty() &&
+                       std::any_of(s->slots.begin(), s->slots.end(), [](const StreamSlot& x) { return !x.busy; });
+            });
+    }
+}
+
+int upload_version(CfServer* s, const CfLightData* host, uint32_t n, LightVersion** out)
+{
+    LightVersion* v = new (std::nothrow) LightVersion();
+    if (!v) return fail(CF_ERROR_OUT_OF_MEMORY, "host allocation");
+    v->count = n;
+    v->d = arena_alloc(s, std::max<size_t>((size_t)n * sizeof(CfLightData), 256));
+    if (!v->d) {
+        delete v;
+        return fail(CF_ERROR_BUDGET, "light set of %u lights does not fit the server's device budget", n);
+    }
+    (void)host;
+    *out = v;
+    return CF_SUCCESS;
+}
+
+// Enqueues the copy that fills v on the upload stream.  Called WITHOUT `mu`:
+// a pageable copy blocks the calling thread, and nothing the worker or a
+// stream callback needs may wait behind it.
+int fill_from_host(CfServer* s, LightVersion* v, const CfLightData* host)
+{
+    DeviceGuard g(s->device);
+    cudaError_t e = cudaEventCreateWithFlags(&v->ready, cudaEventDisableTiming);
+    if (e == cudaSuccess && v->count)
+        e = cudaMemcpyAsync(v->d, host, (size_t)v->count * sizeof(CfLightData), cudaMemcpyHostToDevice, s->upload);
+    if (e == cudaSuccess) e = cudaEventRecord(v->ready, s->upload);
+    return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "light set upload");
+}
+
+void drop_unpublished(CfServer* s, LightVersion* v)
+{
+    s->arena.release(v->d);
+    if (v->ready) cudaEventDestroy(v->ready);
+    delete v;
+    s->memory_epoch++;
+}
+
+void destroy_slot(StreamSlot& sl)
+{
+    if (sl.s) cudaStreamDestroy(sl.s);
+    cudaFree(sl.d_jobs);
+    cudaFree(sl.d_prefix);
+    cudaFree(sl.d_items);
+    cudaFree(sl.d_queues);
+    cudaFreeHost(sl.h_jobs);
+    cudaFreeHost(sl.h_prefix);
+    cudaFreeHost(sl.h_items);
+}
+
+}  // namespace
+
+extern "C" {
+
+int cf_server_create(CfContext* ctx, const CfServerConfig* config, CfServer** out)
+{
+    if (!ctx || !out) return fail(CF_ERROR_INVALID_ARGUMENT, "cf_server_create: null argument");
+    CfServerConfig c{};
+    if (config) c = *config;
+    if (!c.hbm_budget_bytes) c.hbm_budget_bytes = 8ull << 30;
+    if (!c.max_batch_views) c.max_batch_views = 64;
+    if (!c.streams) c.streams = 4;
+    if (!c.max_pending) c.max_pending = 1u << 20;
+    if (!c.max_groups_per_view) c.max_groups_per_view = 16384;
+    if (c.streams > 16 || c.max_batch_views > 4096)
+        return fail(CF_ERROR_INVALID_ARGUMENT, "streams <= 16 and max_batch_views <= 4096");
+    CfServer* s = new (std::nothrow) CfServer();
+    if (!s) return fail(CF_ERROR_OUT_OF_MEMORY, "host allocation");
+    s->ctx = ctx;
+    s->cfg = c;
+    s->device = context_device(ctx);
+    s->dev_error = context_error_word(ctx);
+    s->items_per_slot = c.max_batch_views * c.max_groups_per_view;
+    s->t0 = now_s();
+    DeviceGuard g(s->device);
+    cudaError_t e = cudaMalloc(&s->d_pool, c.hbm_budget_bytes);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->upload, cudaStreamNonBlocking);
+    s->slots.resize(c.streams);
+    for (StreamSlot& sl : s->slots) {
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.s, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_jobs, c.max_batch_views * sizeof(cfk::ViewJob));
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_prefix, 3 * c.max_batch_views * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_items, (size_t)s->items_per_slot * sizeof(uint2));
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_queues, cfk::kMaxBatchQueues * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_jobs, c.max_batch_views * sizeof(cfk::ViewJob));
+        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_prefix, 3 * c.max_batch_views * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_items, (size_t)s->items_per_slot * sizeof(uint2));
+    }
+    if (e != cudaSuccess) {
+        for (StreamSlot& sl : s->slots) destroy_slot(sl);
+        cudaFree(s->d_pool);
+        if (s->upload) cudaStreamDestroy(s->upload);
+        delete s;
+        return cuda_fail(e, "server resources");
+    }
+    s->arena.reset(s->d_pool, c.hbm_budget_bytes);
+    s->worker = std::thread(worker_main, s);
+    *out = s;
+    return CF_SUCCESS;
+}
+
+int cf_server_destroy(CfServer* s)
+{
+    if (!s) return CF_SUCCESS;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+        s->cv.notify_all();
+    }
+    if (s->worker.joinable()) s->worker.join();
+    DeviceGuard g(s->device);
+    cudaDeviceSynchronize();
+    for (auto& d : s->deferred) cudaEventDestroy(d.second);
+    for (auto& kv : s->holding) delete kv.second;
+    for (auto& kv : s->sets) {
+        if (kv.second.cur->ready) cudaEventDestroy(kv.second.cur->ready);
+        delete kv.second.cur;
+    }
+    for (AabbEntry* a : s->aabbs) {
+        if (a->ready) cudaEventDestroy(a->ready);
+        delete a;
+    }
+    for (StreamSlot& sl : s->slots) destroy_slot(sl);
+    cudaStreamDestroy(s->upload);
+    cudaFree(s->d_pool);
+    delete s;
+    return CF_SUCCESS;
+}
+
+int cf_server_register_light_set(CfServer* s, const CfLightData* lights, uint32_t count, uint64_t* id)
+{
+    if (!s || !id || (count && !lights)) return fail(CF_ERROR_INVALID_ARGUMENT, "null argument");
+    if (count > kMaxLights) return fail(CF_ERROR_INVALID_ARGUMENT, "too many lights");
+    LightVersion* v = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        const int st = upload_version(s, lights, count, &v);
+        if (st) return st;
+    }
+    const int st = fill_from_host(s, v, lights);  // not under `mu`
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (st) {
+        drop_unpublished(s, v);
+        return st;
+    }
+    const uint64_t sid = s->next_set++;
+    s->sets[sid] = LightSet{v, ++s->tick};
+    *id = sid;
+    return CF_SUCCESS;
+}
+
+// Publishes v as the current version of set `id` (mu held); v is discarded
+// (once its fill has finished) when the set was released meanwhile.
+int publish_version(CfServer* s, uint64_t id, LightVersion* v, LightVersion* pinned_old)
+{
+    pinned_old->refs--;
+    auto it = s->sets.find(id);
+    if (it == s->sets.end()) {
+        free_version_if_dead(s, pinned_old);
+        s->deferred.emplace_back(v->d, v->ready);  // its fill may still be running
+        delete v;
+        return fail(CF_ERROR_NOT_READY, "light set %llu was released", (unsigned long long)id);
+    }
+    LightVersion* old = it->second.cur;
+    old->retired = true;
+    free_version_if_dead(s, old);
+    if (pinned_old != old) free_version_if_dead(s, pinned_old);
+    it->second.cur = v;
+    it->second.last_use = ++s->tick;
+    return CF_SUCCESS;
+}
+
+int cf_server_update_light_set(CfServer* s, uint64_t id, const CfLightData* lights, uint32_t count)
+{
+    if (!s || (count && !lights)) return fail(CF_ERROR_INVALID_ARGUMENT, "null argument");
+    LightVersion *v = nullptr, *old = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->sets.find(id);
+        if (it == s->sets.end()) return fail(CF_ERROR_NOT_READY, "light set %llu is not resident", (unsigned long long)id);
+        old = it->second.cur;
+        old->refs++;  // neither evictable nor freed while the new version is placed
+        const int st = upload_version(s, lights, count, &v);
+        if (st) {
+            old->refs--;
+            return st;
+        }
+    }
+    const int st = fill_from_host(s, v, lights);  // not under `mu`
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (st) {
+        old->refs--;
+        free_version_if_dead(s, old);
+        drop_unpublished(s, v);
+        return st;
+    }
+    return publish_version(s, id, v, old);
+}
+
+int cf_server_jitter_light_set(CfServer* s, uint64_t id, uint64_t seed, float sigma)
+{
+    if (!s) return fail(CF_ERROR_INVALID_ARGUMENT, "null server");
+    LightVersion *v = nullptr, *old = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->sets.find(id);
+        if (it == s->sets.end()) return fail(CF_ERROR_NOT_READY, "light set %llu is not resident", (unsigned long long)id);
+        old = it->second.cur;
+        old->refs++;  // neither evictable nor freed while the jitter reads it
+        v = new (std::nothrow) LightVersion();
+        unsigned char* d = v ? arena_alloc(s, std::max<size_t>((size_t)old->count * sizeof(CfLightData), 256)) : nullptr;
+        if (!v || !d) {
+            delete v;
+            old->refs--;
+            return fail(CF_ERROR_BUDGET, "no room for a new version of light set %llu", (unsigned long long)id);
+        }
+        v->d = d;
+        v->count = old->count;
+        if (!old->last_read) cudaEventCreateWithFlags(&old->last_read, cudaEventDisableTiming);
+    }
+    cudaError_t e;
+    {
+        DeviceGuard g(s->device);  // not under `mu`
+        e = cudaEventCreateWithFlags(&v->ready, cudaEventDisableTiming);
+        if (e == cudaSuccess && old->ready) e = cudaStreamWaitEvent(s->upload, old->ready, 0);
+        if (e == cudaSuccess)
+            e = cfk::launch_jitter(reinterpret_cast<const CfLightData*>(old->d), reinterpret_cast<CfLightData*>(v->d),
+                                   old->count, seed, sigma, s->upload);
+        if (e == cudaSuccess) e = cudaEventRecord(v->ready, s->upload);
+        if (e == cudaSuccess && old->last_read) e = cudaEventRecord(old->last_read, s->upload);
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (e != cudaSuccess) {
+        old->refs--;
+        free_version_if_dead(s, old);
+        drop_unpublished(s, v);
+        return cuda_fail(e, "light set jitter");
+    }
+    return publish_version(s, id, v, old);
+}
+
+int cf_server_release_light_set(CfServer* s, uint64_t id)
+{
+    if (!s) return fail(CF_ERROR_INVALID_ARGUMENT, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->sets.find(id);
+    if (it == s->sets.end()) return CF_SUCCESS;
+    it->second.cur->retired = true;
+    free_version_if_dead(s, it->second.cur);
+    s->sets.erase(it);
+    s->memory_epoch++;
+    s->cv.notify_all();
+    return CF_SUCCESS;
+}
+
+int cf_server_is_light_set_resident(CfServer* s, uint64_t id, int* resident)
+{
+    if (!s || !resident) return fail(CF_ERROR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    *resident = s->sets.count(id) ? 1 : 0;
+    return CF_SUCCESS;
+}
+
+int cf_server_submit(CfServer* s, const CfServerRequest* req, uint64_t* request_id)
+{
+    if (!s || !req || !request_id) return fail(CF_ERROR_INVALID_ARGUMENT, "cf_server_submit: null argument");
+    uint32_t C = 0;
+    const uint32_t cap = req->max_lights_per_cluster ? req->max_lights_per_cluster : CF_MAX_LIGHTS_PER_CLUSTER_DEFAULT;
+    int st = validate_grid(req->ubo.sliceCountX, req->ubo.sliceCountY, req->ubo.sliceCountZ, cap, &C);
+    if (st) return st;
+    Request* r = new (std::nothrow) Request();
+    if (!r) return fail(CF_ERROR_OUT_OF_MEMORY, "host allocation");
+    r->req = *req;
+    r->req.max_lights_per_cluster = cap;
+    r->clusters = C;
+    r->t_submit = now_s();
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->pending.size() >= s->cfg.max_pending) {
+        delete r;
+        return fail(CF_ERROR_BUDGET, "%zu requests pending", s->pending.size());
+    }
+    auto it = s->sets.find(req->light_set);
+    if (it == s->sets.end()) {
+        delete r;
+        return fail(CF_ERROR_NOT_READY, "light set %llu is not resident", (unsigned long long)req->light_set);
+    }
+    r->lights = it->second.cur;  // this version, whatever updates follow
+    r->lights->refs++;
+    it->second.last_use = ++s->tick;
+    r->id = s->next_req++;
+    *request_id = r->id;
+    s->pending.push_back(r);
+    s->stats.submitted++;
+    s->stats.max_pending = std::max<uint64_t>(s->stats.max_pending, s->pending.size());
+    s->cv.notify_all();
+    return CF_SUCCESS;
+}
+
+int cf_server_poll(CfServer* s, CfServerCompletion* out, uint32_t max, uint32_t* count, int wait_ms)
+{
+    if (!s || !count || (max && !out)) return fail(CF_ERROR_INVALID_ARGUMENT, "null argument");
+    std::unique_lock<std::mutex> lk(s->mu);
+    if (s->completions.empty() && wait_ms > 0)
+        s->done_cv.wait_for(lk, std::chrono::milliseconds(wait_ms), [s] { return !s->completions.empty(); });
+    uint32_t n = 0;
+    while (n < max && !s->completions.empty()) {
+        out[n++] = s->completions.front();
+        s->completions.pop_front();
+    }
+    *count = n;
+    return CF_SUCCESS;
+}
+
+int cf_server_release(CfServer* s, uint64_t request_id)
+{
+    if (!s) return fail(CF_ERROR_INVALID_ARGUMENT, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->holding.find(request_id);
+    if (it == s->holding.end()) return fail(CF_ERROR_INVALID_ARGUMENT, "request %llu holds no outputs",
+                                            (unsigned long long)request_id);
+    s->arena.release(it->second->out);
+    delete it->second;
+    s->holding.erase(it);
+    s->memory_epoch++;
+    s->cv.notify_all();
+    return CF_SUCCESS;
+}
+
+int cf_server_set_tuning(CfServer* s, uint32_t slice_clusters, int clusters_per_warp, int warps, int tile, int stages)
+{
+    if (!s) return fail(CF_ERROR_INVALID_ARGUMENT, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (clusters_per_warp == 0) {
+        s->tuned.erase(slice_clusters);
+        return CF_SUCCESS;
+    }
+    const cfk::CullConfig c{clusters_per_warp, warps, tile, stages, 1};
+    if (!cfk::cull_config_supported(c)) return fail(CF_ERROR_INVALID_ARGUMENT, "unsupported configuration");
+    s->tuned[slice_clusters] = c;
+    return CF_SUCCESS;
+}
+
+int cf_server_get_stats(CfServer* s, CfServerStats* out)
+{
+    if (!s || !out) return fail(CF_ERROR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->stats;
+    out->arena_used_bytes = s->arena.used();
+    out->arena_bytes = s->arena.size();
+    out->pending = s->pending.size();
+    out->resident_light_sets = s->sets.size();
+    out->resident_projections = s->aabbs.size();
+    return CF_SUCCESS;
+}
+
+}  // extern "C"

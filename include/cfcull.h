@@ -251,6 +251,107 @@ CFCULL_API int cf_batch_autotune(CfBatch* batch, int repeats, void* stream);
 CFCULL_API int cf_batch_get_info(const CfBatch* batch, CfBatchInfo* info);
 
 /* ------------------------------------------------------------------------ */
+/* Server: culling requests admitted as they arrive (continuous batching).    */
+/* No counterpart in the reference.  A request names a view (UBO) and a light */
+/* set resident on the device; the server keeps light sets and the AABBs of   */
+/* each projection resident, admits requests in arrival order within a fixed  */
+/* device-memory budget, and launches every admissible pending request as one */
+/* batch whenever one of its streams is free, so batches overlap on the GPU.  */
+/* ------------------------------------------------------------------------ */
+typedef struct CfServer CfServer;
+
+typedef struct CfServerConfig {
+    uint64_t hbm_budget_bytes;     /* device memory for light sets, AABBs, scratch and outputs (default 8 GiB) */
+    uint32_t max_batch_views;      /* views per launch (default 64)                                         */
+    uint32_t streams;              /* batches in flight at once (default 4)                                  */
+    uint32_t max_pending;          /* submissions waiting for admission (default 2^20)                      */
+    uint32_t max_groups_per_view;  /* largest view, in cluster groups (default 16384)                        */
+} CfServerConfig;
+
+typedef struct CfServerRequest {
+    CfClusterForwardUBO ubo;
+    uint64_t light_set;              /* id from cf_server_register_light_set            */
+    uint64_t user_tag;               /* returned in the completion                      */
+    uint32_t max_lights_per_cluster; /* 0 = 150                                         */
+    uint32_t _pad[3];
+} CfServerRequest;
+
+typedef struct CfServerCompletion {
+    uint64_t request_id, user_tag;
+    int32_t status;                  /* CF_SUCCESS, CF_ERROR_NOT_READY (light set not resident), CF_ERROR_BUDGET ... */
+    uint32_t clusters;
+    double t_submit, t_launch, t_complete; /* seconds since the server was created (host steady clock) */
+    const CfLightCell* d_cells;      /* device results, valid until cf_server_release   */
+    const uint32_t* d_indices;
+    const uint32_t* d_total;
+} CfServerCompletion;
+
+typedef struct CfServerStats {
+    uint64_t submitted, completed, batches, views_launched, max_pending, evictions;
+    uint64_t arena_bytes, arena_used_bytes, arena_peak_bytes, pending, resident_light_sets, resident_projections;
+    uint32_t max_batch_views, _pad;
+} CfServerStats;
+
+CFCULL_API int cf_server_create(CfContext* ctx, const CfServerConfig* config, CfServer** out);
+/* Finishes every submitted request, then frees everything. */
+CFCULL_API int cf_server_destroy(CfServer* server);
+/* Uploads a light set (device memory from the budget; CF_ERROR_BUDGET if it
+ * cannot fit).  Sets no submitted request uses are evicted least recently
+ * used when admission needs room; submitting against an evicted set returns
+ * CF_ERROR_NOT_READY (register it again). */
+CFCULL_API int cf_server_register_light_set(CfServer* server, const CfLightData* lights, uint32_t count, uint64_t* id);
+/* Replaces a set's lights for requests submitted from now on (copy on write:
+ * a request binds the set's version current when it is submitted). */
+CFCULL_API int cf_server_update_light_set(CfServer* server, uint64_t id, const CfLightData* lights, uint32_t count);
+/* Moves every light of a set on the device, copy on write like an update:
+ * position += sigma * (s - 6), s the sum of 12 uniforms in [0, 1) drawn from
+ * a splitmix64 hash of (seed + light * 0x9E3779B97F4A7C15 + (axis * 12 + term)
+ * * 0xD1B54A32D192ED03), u = (hash >> 40) * 2^-24, every operation rounded
+ * to nearest in that order, so a host can reproduce the result bit for bit. */
+CFCULL_API int cf_server_jitter_light_set(CfServer* server, uint64_t id, uint64_t seed, float sigma);
+CFCULL_API int cf_server_release_light_set(CfServer* server, uint64_t id);
+CFCULL_API int cf_server_is_light_set_resident(CfServer* server, uint64_t id, int* resident);
+/* Thread-safe. */
+CFCULL_API int cf_server_submit(CfServer* server, const CfServerRequest* request, uint64_t* request_id);
+/* Up to `max` completions, waiting up to wait_ms for the first one. */
+CFCULL_API int cf_server_poll(CfServer* server, CfServerCompletion* out, uint32_t max, uint32_t* count, int wait_ms);
+/* Returns a completed request's device results to the budget. */
+CFCULL_API int cf_server_release(CfServer* server, uint64_t request_id);
+CFCULL_API int cf_server_set_tuning(CfServer* server, uint32_t slice_clusters, int clusters_per_warp, int warps,
+                                    int tile, int stages);
+CFCULL_API int cf_server_get_stats(CfServer* server, CfServerStats* stats);
+
+/* A served stream replayed in real time against a server (load driver for
+ * measurement): Poisson arrivals at rate_per_s for duration_s; each request
+ * takes one of the projections (its cameraView is replaced by a look-at from
+ * an eye uniform in [eye_lo, eye_hi] to a target uniform in
+ * [target_lo, target_hi]) and, with probability p_reuse, one of its
+ * submitting thread's recent light sets moved by cf_server_jitter_light_set
+ * (sigma jitter_sigma), else a new set copied from base_sets.  recent_sets
+ * is split across submit_threads; sets leaving a window are released. */
+typedef struct CfServeLoad {
+    double rate_per_s, duration_s, p_reuse;
+    uint64_t seed;
+    float jitter_sigma;
+    uint32_t recent_sets, submit_threads, max_lights_per_cluster;
+    uint32_t n_projections, n_base_sets;
+    const CfClusterForwardUBO* projections;
+    const CfLightData* const* base_sets;
+    const uint32_t* base_counts;
+    float eye_lo[3], eye_hi[3], target_lo[3], target_hi[3];
+} CfServeLoad;
+
+typedef struct CfServeReport {
+    uint64_t scheduled, submitted, completed, failed, new_sets, reused_sets, tests_brute_force;
+    double wall_s, offered_rate, achieved_rate;
+    double latency_p50_ms, latency_p90_ms, latency_p99_ms, latency_p999_ms, latency_max_ms; /* arrival -> done */
+    double queue_p50_ms, queue_p99_ms;                                                     /* arrival -> launch */
+    double submit_lag_p99_ms;                                                              /* arrival -> submit */
+} CfServeReport;
+
+CFCULL_API int cf_serve_run_load(CfServer* server, const CfServeLoad* load, CfServeReport* report);
+
+/* ------------------------------------------------------------------------ */
 /* Stateless entry points on caller-owned device memory.                     */
 /* ------------------------------------------------------------------------ */
 

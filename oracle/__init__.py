@@ -120,3 +120,25 @@ class Reference:
                                lights.shape[0], cells.ctypes.data, idx.ctypes.data, cap_total, C.byref(total), threads)
         assert st == 0, st
         return cells, idx[: total.value].copy()
+
+
+def jitter_lights(lights: np.ndarray, seed: int, sigma: float) -> np.ndarray:
+    """Host restatement of the server's light jitter (cf_server_jitter_light_set,
+    hellovulkan_gb300/csrc/cf_kernels.cu jitter_kernel), bit for bit."""
+    L = np.array(lights, np.float32, copy=True).reshape(-1, 12)
+    n = L.shape[0]
+    i = np.arange(n, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        for a in range(3):
+            s = np.zeros(n, np.float32)
+            for k in range(12):
+                x = np.uint64(seed) + i * np.uint64(0x9E3779B97F4A7C15) + np.uint64(a * 12 + k) * np.uint64(
+                    0xD1B54A32D192ED03)
+                x ^= x >> np.uint64(30)
+                x *= np.uint64(0xBF58476D1CE4E5B9)
+                x ^= x >> np.uint64(27)
+                x *= np.uint64(0x94D049BB133111EB)
+                x ^= x >> np.uint64(31)
+                s = s + (x >> np.uint64(40)).astype(np.float32) * np.float32(2.0 ** -24)
+            L[:, a] = L[:, a] + np.float32(sigma) * (s - np.float32(6.0))
+    return L

@@ -1,0 +1,137 @@
+"""GPU tests of the culling server: results against the oracle, the same
+bits alone and in a concurrent mix, copy-on-write light updates and device
+jitter (checked against its host restatement), budget admission and
+eviction, and a short run of the Poisson load driver."""
+import numpy as np
+import pytest
+
+from hellovulkan_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_result(oracle, ubo, lights, cap=150):
+    a = oracle.generate_aabbs(ubo)
+    cells, idx, _ = oracle.cull(ubo, a, lights, cap)
+    return cells, idx
+
+
+def take(srv, count):
+    out = srv.wait_all(count)
+    assert len(out) == count
+    return {c.request_id: c for c in out}
+
+
+def test_server_results_match_the_oracle(gpu, oracle):
+    from hellovulkan_gb300.server import Server
+    srv = Server(gpu, budget_bytes=1 << 30)
+    rng = np.random.default_rng(1)
+    views = [scenes.batch_view(rng) for _ in range(6)]
+    reqs = {}
+    for v in views:
+        lights = v.lights[:4000]
+        sid = srv.register(lights)
+        reqs[srv.submit(v.ubo, sid)] = (v.ubo, lights)
+    for rid, c in take(srv, len(reqs)).items():
+        assert c.status == 0
+        cells, idx = srv.read(c)
+        oc, oi = oracle_result(oracle, *reqs[rid])
+        assert np.array_equal(cells, oc) and np.array_equal(idx, oi)
+        srv.release(rid)
+    st = srv.stats()
+    assert st["completed"] == len(views) and st["resident_projections"] >= 1
+    srv.close()
+
+
+def test_same_result_alone_and_in_a_concurrent_mix(gpu, oracle):
+    from hellovulkan_gb300.server import Server
+    srv = Server(gpu, budget_bytes=2 << 30, max_batch_views=16, streams=4)
+    rng = np.random.default_rng(2)
+    probe = scenes.batch_view(rng)
+    probe_lights = probe.lights[:5000]
+    sid = srv.register(probe_lights)
+    # alone
+    rid = srv.submit(probe.ubo, sid)
+    c = take(srv, 1)[rid]
+    alone = srv.read(c)
+    srv.release(rid)
+    # in a mix: 120 other requests around it, over several batches and streams
+    others = []
+    for k in range(60):
+        v = scenes.batch_view(rng)
+        others.append((v.ubo, srv.register(v.lights[:3000])))
+    ids = [srv.submit(u, s) for u, s in others[:40]]
+    rid2 = srv.submit(probe.ubo, sid)
+    ids += [srv.submit(u, s) for u, s in others[40:]] + [srv.submit(u, s) for u, s in others]
+    done = take(srv, len(ids) + 1)
+    mixed = srv.read(done[rid2])
+    for r in done:
+        srv.release(r)
+    assert np.array_equal(alone[0], mixed[0]) and np.array_equal(alone[1], mixed[1])
+    oc, oi = oracle_result(oracle, probe.ubo, probe_lights)
+    assert np.array_equal(mixed[0], oc) and np.array_equal(mixed[1], oi)
+    assert srv.stats()["batches"] >= 2
+    srv.close()
+
+
+def test_copy_on_write_updates_and_device_jitter(gpu, oracle):
+    from hellovulkan_gb300.server import Server
+    from oracle import jitter_lights
+    srv = Server(gpu, budget_bytes=1 << 30)
+    v = scenes.plain_small(3)
+    sid = srv.register(v.lights)
+    r1 = srv.submit(v.ubo, sid)
+    moved = v.lights.copy()
+    moved[:, :3] += 0.75
+    srv.update(sid, moved)  # r1 keeps the version it was submitted with
+    r2 = srv.submit(v.ubo, sid)
+    srv.jitter(sid, 1234, 0.1)
+    r3 = srv.submit(v.ubo, sid)
+    done = take(srv, 3)
+    res = {r: srv.read(done[r]) for r in (r1, r2, r3)}
+    for r in done:
+        srv.release(r)
+    oc, oi = oracle_result(oracle, v.ubo, v.lights)
+    assert np.array_equal(res[r1][0], oc) and np.array_equal(res[r1][1], oi)
+    oc, oi = oracle_result(oracle, v.ubo, moved)
+    assert np.array_equal(res[r2][0], oc) and np.array_equal(res[r2][1], oi)
+    jittered = jitter_lights(moved, 1234, 0.1)
+    assert not np.array_equal(jittered, moved)
+    oc, oi = oracle_result(oracle, v.ubo, jittered)
+    assert np.array_equal(res[r3][0], oc) and np.array_equal(res[r3][1], oi)
+    srv.close()
+
+
+def test_budget_admission_and_eviction(gpu):
+    from hellovulkan_gb300 import CfError
+    from hellovulkan_gb300.server import Server
+    srv = Server(gpu, budget_bytes=40 << 20, max_batch_views=4, streams=2)
+    rng = np.random.default_rng(3)
+    big = scenes.plain_large(2)  # its scratch and outputs alone (about 51 MB) exceed 40 MiB
+    sid = srv.register(big.lights)
+    rid = srv.submit(big.ubo, sid)
+    c = take(srv, 1)[rid]
+    assert c.status == 7  # CF_ERROR_BUDGET
+    # many small sets: the oldest unused ones are evicted to make room
+    small = [scenes.uniform_box_lights(rng, 60000, [-20, 0, -40], [20, 15, 10]) for _ in range(40)]
+    ids = [srv.register(s) for s in small]
+    assert srv.stats()["evictions"] > 0 and not srv.resident(ids[0]) and srv.resident(ids[-1])
+    v = scenes.plain_small(1)
+    with pytest.raises(CfError) as e:
+        srv.submit(v.ubo, ids[0])  # evicted
+    assert e.value.status == 5  # CF_ERROR_NOT_READY
+    with pytest.raises(CfError):
+        srv.register(np.zeros((2_000_000, 12), np.float32))  # larger than the whole budget
+    srv.close()
+
+
+def test_load_driver_completes_every_request(gpu):
+    from hellovulkan_gb300.server import Server, run_load
+    srv = Server(gpu, budget_bytes=4 << 30)
+    rng = np.random.default_rng(9)
+    base = [scenes.blob_lights(rng, int(n)) for n in (256, 1000, 4000, 12000)]
+    rep = run_load(srv, rate=2000.0, duration=0.5, base_sets=base, submit_threads=2)
+    assert rep["scheduled"] > 500 and rep["completed"] == rep["submitted"] and rep["failed"] == 0
+    assert rep["latency_p50_ms"] > 0 and rep["latency_p99_ms"] >= rep["latency_p50_ms"]
+    assert rep["reused_sets"] > 0 and rep["new_sets"] > 0
+    srv.close()

@@ -62,6 +62,12 @@ def parse():
     p.add_argument("--tuning", type=str, default="", help="K,warps,tile,stages,binned of the culling kernel")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-batch", action="store_true", help="skip the 256-view batched measurement")
+    p.add_argument("--no-serve", action="store_true", help="skip the served-stream measurement")
+    p.add_argument("--serve-seconds", type=float, default=10.0, help="length of each served-stream run")
+    p.add_argument("--no-stress", action="store_true", help="skip the animated many-view measurement")
+    p.add_argument("--stress-views", type=int, default=4096)
+    p.add_argument("--stress-lights", type=int, default=4096)
+    p.add_argument("--stress-frames", type=int, default=600)
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline budget")
     return p.parse_args()
 
@@ -270,6 +276,32 @@ def measure_batch(ctx, stream, n_views=256, passes=20, seed=3, sample_views=6):
 
     per_view_pass()
     per_view_ms = timed(per_view_pass, 3)
+
+    # the plain brute-force kernel (every light against every cluster), one
+    # pipeline and one launch sequence per view, as the reference records one
+    # LightCulling dispatch per view
+    from hellovulkan_gb300.pipelines import (PipelineAABBGenerator, PipelineLightCulling, ResourcesClusterForward,
+                                             ResourcesLight)
+    plain = []
+    for v in views:
+        rl = ResourcesLight(ctx)
+        rl.add_lights(v.lights)
+        rc = ResourcesClusterForward(ctx)
+        rc.create_buffers(*v.grid, v.cap)
+        gen = PipelineAABBGenerator(ctx, rc)
+        gen.set_cluster_forward_ubo(v.ubo)
+        gen.fill_command_buffer(stream)
+        cu = PipelineLightCulling(ctx, rl, rc)
+        cu.set_cluster_forward_ubo(v.ubo)
+        cu.set_tuning(*(PLAIN_SMALL if v.clusters <= 8192 else PLAIN_LARGE))
+        plain.append((rl, rc, gen, cu))
+
+    def plain_pass():
+        for _, _, _, cu in plain:
+            cu.fill_command_buffer(stream)
+
+    plain_pass()
+    plain_ms = timed(plain_pass, 3)
     b.cull(stream)  # leave the batch's own outputs in the buffers for the parity check
     torch.cuda.synchronize()
 
@@ -285,8 +317,13 @@ def measure_batch(ctx, stream, n_views=256, passes=20, seed=3, sample_views=6):
         oc, oi, _ = o.cull(views[i].ubo, oa, views[i].lights, views[i].cap)
         parity &= bool(np.array_equal(a.view(np.uint32), oa.view(np.uint32)) and np.array_equal(cells, oc)
                        and np.array_equal(idx, oi))
+        pc, pi = plain[i][1].read_outputs(stream)
+        parity &= bool(np.array_equal(pc, oc) and np.array_equal(pi, oi))
+    for objs in plain:
+        for o_ in reversed(objs):
+            o_.close()
     tests = sum(v.clusters * v.light_count for v in views)
-    bm, pm = float(np.mean(batch_ms)), float(np.mean(per_view_ms))
+    bm, pm, plm = float(np.mean(batch_ms)), float(np.mean(per_view_ms)), float(np.mean(plain_ms))
     info = b.info()
     b.close()
     return {
@@ -297,10 +334,79 @@ def measure_batch(ctx, stream, n_views=256, passes=20, seed=3, sample_views=6):
         "tests_per_s": tests / (bm * 1e-3),
         "per_view_launch_ms": pm, "per_view_launch_views_per_s": n_views / (pm * 1e-3),
         "speedup_vs_per_view_launch": pm / bm,
+        "plain_per_view_ms": plm, "plain_per_view_views_per_s": n_views / (plm * 1e-3),
+        "speedup_vs_plain_per_view": plm / bm,
+        "per_view_note": "per_view_launch: cf_cull_lights (binned) once per view; plain_per_view: the brute-force "
+                         "kernel through PipelineLightCulling once per view",
         "passes": passes, "graph": True, "autotune_s": tune_s, "buckets": info["bucket_configs"],
         "items": info["items"], "parity_sampled_views": parity, "sampled_views": sample,
         "l2": "inputs larger than L2 (%.0f MB of buffers), no flush" % (bufs.device_bytes / 1e6),
     }
+
+
+def measure_serve(ctx, seconds, rates=(2000.0, 10000.0, 50000.0), saturation_rate=200000.0,
+                  saturation_seconds=2.0, submit_threads=4):
+    """The served stream: Poisson arrivals at each rate for `seconds`, requests
+    drawn like the batched mix (4 projections, random cameras, 128 base light
+    sets of 256..65536 blob lights), light sets re-referenced with p = 0.7 and
+    jittered on the device by N(0, 0.1) per request, an 8 GiB device budget.
+    Latency runs from the scheduled arrival to the completion callback.  A last
+    run offers far more than the server can take, to measure its capacity."""
+    from hellovulkan_gb300.server import Server, run_load
+    keep = ("offered_rate", "achieved_rate", "scheduled", "completed", "failed", "latency_p50_ms", "latency_p90_ms",
+            "latency_p99_ms", "latency_p999_ms", "queue_p50_ms", "queue_p99_ms", "exec_p50_ms", "exec_p99_ms",
+            "submit_lag_p99_ms", "register_call_p50_us", "jitter_call_p50_us", "submit_call_p50_us", "tests_per_s",
+            "new_sets", "reused_sets")
+    runs = []
+    for rate, dur, thr in [(r, seconds, submit_threads) for r in rates] + [(saturation_rate, saturation_seconds, 8)]:
+        srv = Server(ctx, budget_bytes=8 << 30, max_batch_views=64, streams=4)
+        rep = run_load(srv, rate=rate, duration=dur, submit_threads=thr)
+        st = srv.stats()
+        srv.close()
+        r = {"rate": rate, "seconds": dur, "submit_threads": thr}
+        r.update({k: rep[k] for k in keep})
+        r.update({"views_per_s": rep["achieved_rate"], "batches": st["batches"],
+                  "mean_views_per_batch": st["views_launched"] / max(1, st["batches"]),
+                  "max_batch_views": st["max_batch_views"], "arena_peak_bytes": st["arena_peak_bytes"],
+                  "evictions": st["evictions"], "p99_within_2ms": rep["latency_p99_ms"] <= 2.0})
+        runs.append(r)
+    return {"workload": "Poisson arrivals, 4 projections {8x8x16,16x9x24,24x14x32,32x18x48}, 128 base sets of "
+                        "256..65536 blob lights, p_reuse 0.7 with device jitter sigma 0.1, 8 GiB budget, "
+                        "64 views per batch, 4 streams",
+            "runs": runs[:-1], "saturation": runs[-1], "capacity_views_per_s": runs[-1]["achieved_rate"]}
+
+
+def measure_stress(ctx, stream, n_views, n_lights, frames, seed=5):
+    """The animated workload: n_views views x n_lights lights, every light moved
+    one step along its orbit in place on the device each frame, every view
+    culled each frame in one batched pass; the projection of every view changes
+    every 60 frames (grid 16x9x24 <-> 32x18x48, fovY 45 <-> 60 degrees), which
+    regenerates all AABBs.  Sampled frames and views are checked against the
+    oracle (lights against the host restatement of the animation)."""
+    import torch
+
+    from hellovulkan_gb300.stress import StressAnimation, stress_device_bytes
+    from oracle import Oracle
+    free, _ = torch.cuda.mem_get_info()
+    need = stress_device_bytes(n_views, n_lights) + n_views // 2 * (4_200_000 + 20_800_000) * n_lights // 4096
+    if need > 0.8 * free:
+        return {"skipped": "needs about %.1f GB of device memory, %.1f GB free" % (need / 1e9, free / 1e9)}
+    t0 = time.perf_counter()
+    st = StressAnimation(ctx, n_views=n_views, n_lights=n_lights, seed=seed)
+    setup_s = time.perf_counter() - t0
+    check_frames = {f for f in (0, 59, 60, 61, 299, frames - 1) if 0 <= f < frames}
+    check_views = sorted({0, 1, n_views // 2 + 1, n_views - 1})
+    rep = st.run(frames, stream, check_frames=check_frames, check_views=check_views, oracle=Oracle())
+    st.close()
+    del st
+    torch.cuda.empty_cache()
+    rep["setup_s"] = setup_s
+    rep["device_bytes"] = need
+    rep["workload"] = ("%d views x %d lights, %d frames, projection change every 60 frames (grids 16x9x24 / "
+                       "32x18x48 alternating per view and per epoch, fovY 45 / 60), lights on circles r U[1,10], "
+                       "omega U[0.1,2] rad/s at 60 Hz, moved in place on the device" % (n_views, n_lights, frames))
+    rep["l2"] = "inputs larger than L2 (%.0f MB of lights per frame), no flush" % (n_views * n_lights * 48 / 1e6)
+    return rep
 
 
 def run_ours(args):
@@ -412,6 +518,16 @@ def run_ours(args):
     batched = None
     if not args.no_batch and rank == 0:
         batched = measure_batch(ctx, stream)
+    stress = None
+    if not args.no_stress and rank == 0:
+        stress = measure_stress(ctx, stream, args.stress_views, args.stress_lights, args.stress_frames)
+    served = None
+    if not args.no_serve and rank == 0:
+        served = measure_serve(ctx, args.serve_seconds)
+        if batched:
+            served["speedup_vs_plain_per_view"] = served["capacity_views_per_s"] / batched["plain_per_view_views_per_s"]
+            served["speedup_vs_per_view_launch"] = (served["capacity_views_per_s"] /
+                                                    batched["per_view_launch_views_per_s"])
 
     tests_per_view = view.clusters * view.light_count
     stats = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device="cuda")
@@ -501,6 +617,8 @@ def run_ours(args):
         "gpu_launches": 4 * (args.steps + e2e_steps),
         "clocks": clocks,
         "batched": batched,
+        "served": served,
+        "stress": stress,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:

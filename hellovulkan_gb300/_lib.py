@@ -29,6 +29,10 @@ class CfLightCell(C.Structure):
     _fields_ = [("offset", C.c_uint32), ("count", C.c_uint32)]
 
 
+class CfLightOrbit(C.Structure):
+    _fields_ = [("offset", C.c_float * 2), ("rot", C.c_float * 2), ("center", C.c_float * 4)]
+
+
 class CfClusterForwardUBO(C.Structure):
     _fields_ = [
         ("cameraInverseProjection", C.c_float * 16),
@@ -121,15 +125,18 @@ class CfServeReport(C.Structure):
                                           "reused_sets", "tests_brute_force")] + [
         (n, C.c_double) for n in ("wall_s", "offered_rate", "achieved_rate", "latency_p50_ms", "latency_p90_ms",
                                   "latency_p99_ms", "latency_p999_ms", "latency_max_ms", "queue_p50_ms",
-                                  "queue_p99_ms", "submit_lag_p99_ms")]
+                                  "queue_p99_ms", "submit_lag_p99_ms", "exec_p50_ms", "exec_p99_ms",
+                                  "register_call_p50_us", "register_call_p99_us", "jitter_call_p50_us",
+                                  "jitter_call_p99_us", "submit_call_p50_us", "submit_call_p99_us")]
 
 
 assert C.sizeof(CfServerConfig) == 24 and C.sizeof(CfServerRequest) == 208
 assert C.sizeof(CfServerCompletion) == 72 and C.sizeof(CfServerStats) == 104
-assert C.sizeof(CfServeLoad) == 128 and C.sizeof(CfServeReport) == 144
+assert C.sizeof(CfServeLoad) == 128 and C.sizeof(CfServeReport) == 208
 assert CfServeLoad.projections.offset == 56 and CfServeLoad.eye_lo.offset == 80
 assert C.sizeof(CfBatchView) == 240 and C.sizeof(CfBatchInfo) == 216
 assert C.sizeof(CfLightData) == 48 and C.sizeof(CfAABB) == 32 and C.sizeof(CfLightCell) == 8
+assert C.sizeof(CfLightOrbit) == 32
 assert C.sizeof(CfClusterForwardUBO) == 176
 
 STATUS = {
@@ -190,6 +197,7 @@ _SIGS = {
     "cf_pipeline_light_culling_read_work_counters": [_P, _PU64],
     "cf_cull_workspace_size": [C.POINTER(CfClusterForwardUBO), _U32, _U32, _PU64],
     "cf_generate_aabbs": [C.POINTER(CfClusterForwardUBO), _P, _P],
+    "cf_animate_light_orbits": [_P, _P, _U64, _U32, _P],
     "cf_cull_lights": [C.POINTER(CfClusterForwardUBO), _P, _P, _U32, _U32, _P, _P, _U64, _P, _P, _U64, _P],
     "cf_cull_workspace_device_error": [_P, _PU32],
     "cf_cull_lights_static_scratch": [C.POINTER(CfClusterForwardUBO), _P, _P, _U32, _U32, _P, _P, _U64, _P, _P, _P],

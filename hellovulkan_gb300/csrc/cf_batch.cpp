@@ -73,6 +73,11 @@ struct CfBatch {
     uint32_t* d_queues = nullptr;
     unsigned char* d_ws = nullptr;
     size_t ws_cap = 0;
+    cfk::AabbJob* d_aabb_jobs = nullptr;  // one AABB-generator record per view
+    size_t aabb_jobs_cap = 0;
+    uint32_t* d_aabb_prefix = nullptr;    // first block of each view in the AABB launch
+    size_t aabb_prefix_cap = 0;
+    uint32_t aabb_blocks = 0;
     // graph
     bool use_graph = true;
     cudaGraphExec_t exec = nullptr;
@@ -115,7 +120,9 @@ int rebuild(CfBatch* b)
     b->jobs.assign(n, cfk::ViewJob{});
     std::vector<size_t> ws_off(n);
     std::vector<cfk::WorkspaceLayout> lay(n);
-    std::vector<uint32_t> prefix(3 * (size_t)n);
+    std::vector<uint32_t> prefix(3 * (size_t)n), aabb_prefix(n);
+    std::vector<cfk::AabbJob> aabb_jobs(n);
+    uint32_t ab = 0;
     size_t ws = 0;
     uint32_t xb = 0, bb = 0, cb = 0;
     for (uint32_t i = 0; i < n; ++i) {
@@ -149,6 +156,9 @@ int rebuild(CfBatch* b)
         prefix[i] = xb;
         prefix[n + i] = bb;
         prefix[2 * (size_t)n + i] = cb;
+        aabb_jobs[i] = cfk::AabbJob{bv.ubo, bv.d_aabbs, 0};
+        aabb_prefix[i] = ab;
+        ab += (C + 255) / 256;
         xb += cfk::granules(j.v.lpad);
         bb += Z;
         cb += cfk::copy_blocks(C);
@@ -156,6 +166,7 @@ int rebuild(CfBatch* b)
     b->xform_blocks = xb;
     b->bin_blocks = bb;
     b->copy_blocks_total = cb;
+    b->aabb_blocks = ab;
     b->ws_bytes = ws;
     DeviceGuard g(b->device);
     int s = grow(reinterpret_cast<void**>(&b->d_ws), &b->ws_cap, std::max<size_t>(ws, 256), "batch workspace");
@@ -200,12 +211,16 @@ int rebuild(CfBatch* b)
     s = grow(reinterpret_cast<void**>(&b->d_jobs), &b->jobs_cap, std::max<size_t>(n, 1) * sizeof(cfk::ViewJob), "batch jobs");
     if (!s) s = grow(reinterpret_cast<void**>(&b->d_prefix), &b->prefix_cap, std::max<size_t>(3 * (size_t)n, 1) * 4, "batch prefix");
     if (!s) s = grow(reinterpret_cast<void**>(&b->d_items), &b->items_cap, std::max<size_t>(items.size(), 1) * sizeof(uint2), "batch items");
+    if (!s) s = grow(reinterpret_cast<void**>(&b->d_aabb_jobs), &b->aabb_jobs_cap, std::max<size_t>(n, 1) * sizeof(cfk::AabbJob), "batch AABB jobs");
+    if (!s) s = grow(reinterpret_cast<void**>(&b->d_aabb_prefix), &b->aabb_prefix_cap, std::max<size_t>(n, 1) * 4, "batch AABB prefix");
     if (s) return s;
     cudaError_t e = cudaSuccess;
     if (n) e = cudaMemcpy(b->d_jobs, b->jobs.data(), n * sizeof(cfk::ViewJob), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && n) e = cudaMemcpy(b->d_prefix, prefix.data(), prefix.size() * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !items.empty())
         e = cudaMemcpy(b->d_items, items.data(), items.size() * sizeof(uint2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n) e = cudaMemcpy(b->d_aabb_jobs, aabb_jobs.data(), n * sizeof(cfk::AabbJob), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n) e = cudaMemcpy(b->d_aabb_prefix, aabb_prefix.data(), n * 4, cudaMemcpyHostToDevice);
     return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "batch tables upload");
 }
 
@@ -294,6 +309,8 @@ int cf_batch_destroy(CfBatch* b)
     cudaFree(b->d_items);
     cudaFree(b->d_queues);
     cudaFree(b->d_ws);
+    cudaFree(b->d_aabb_jobs);
+    cudaFree(b->d_aabb_prefix);
     delete b;
     return CF_SUCCESS;
 }
@@ -325,11 +342,9 @@ int cf_batch_generate_aabbs(CfBatch* b, void* stream)
 {
     if (!b) return fail(CF_ERROR_INVALID_ARGUMENT, "null batch");
     DeviceGuard g(b->device);
-    for (const CfBatchView& v : b->views) {
-        cudaError_t e = cfk::launch_aabb(v.ubo, v.d_aabbs, (cudaStream_t)stream);
-        if (e != cudaSuccess) return cuda_fail(e, "AABB generator launch");
-    }
-    return CF_SUCCESS;
+    const cudaError_t e = cfk::launch_batch_aabb(b->d_aabb_jobs, b->d_aabb_prefix, (uint32_t)b->views.size(),
+                                                 b->aabb_blocks, (cudaStream_t)stream);
+    return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "AABB generator launch");
 }
 
 int cf_batch_cull(CfBatch* b, void* stream)

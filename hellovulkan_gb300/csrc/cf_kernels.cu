@@ -161,11 +161,8 @@ __device__ __forceinline__ ViewPoint ray_z(const ViewPoint& p, float z)
     return {cf_fdiv(cf_fmul(p.x, z), p.z), cf_fdiv(cf_fmul(p.y, z), p.z), cf_fdiv(cf_fmul(p.z, z), p.z)};
 }
 
-__global__ void __launch_bounds__(256) aabb_kernel(const CfClusterForwardUBO ubo, float4* __restrict__ out,
-                                                   uint32_t clusters)
+__device__ __forceinline__ void aabb_body(const CfClusterForwardUBO& ubo, float4* __restrict__ out, uint32_t c)
 {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= clusters) return;
     const uint32_t X = ubo.sliceCountX, Y = ubo.sliceCountY, Z = ubo.sliceCountZ;
     const uint32_t i = c % X, j = (c / X) % Y, k = c / (X * Y);
     const float npx = cf_fdiv(1.0f, (float)X);
@@ -190,6 +187,13 @@ __global__ void __launch_bounds__(256) aabb_kernel(const CfClusterForwardUBO ubo
     hi.w = 0.0f;
     out[2 * (size_t)c] = lo;
     out[2 * (size_t)c + 1] = hi;
+}
+
+__global__ void __launch_bounds__(256) aabb_kernel(const CfClusterForwardUBO ubo, float4* __restrict__ out,
+                                                   uint32_t clusters)
+{
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < clusters) aabb_body(ubo, out, c);
 }
 
 // ---------------------------------------------------------------------------
@@ -254,6 +258,18 @@ __global__ void __launch_bounds__(kFlagGranule) batch_xform_kernel(const ViewJob
     const ViewJob& j = jobs[vi];
     light_xform_body(j.lights, j.light_count, j.v.lpad, j.view, const_cast<float4*>(j.v.vlights),
                      const_cast<uint32_t*>(j.v.nonfinite), blockIdx.x - __ldg(&prefix[vi]));
+}
+
+// Batched AABB generator: block b holds clusters [256 (b - prefix[v]), +256)
+// of view v.
+__global__ void __launch_bounds__(256) batch_aabb_kernel(const AabbJob* __restrict__ jobs,
+                                                         const uint32_t* __restrict__ prefix, uint32_t n_views)
+{
+    const uint32_t vi = find_view(prefix, n_views, blockIdx.x);
+    const AabbJob& j = jobs[vi];
+    const uint32_t c = (blockIdx.x - __ldg(&prefix[vi])) * 256 + threadIdx.x;
+    if (c < j.ubo.sliceCountX * j.ubo.sliceCountY * j.ubo.sliceCountZ)
+        aabb_body(j.ubo, reinterpret_cast<float4*>(j.out), c);
 }
 
 // ---------------------------------------------------------------------------
@@ -1136,6 +1152,32 @@ __global__ void __launch_bounds__(256) jitter_kernel(const CfLightData* __restri
     dst[i] = L;
 }
 
+// Moves each light `frames` steps along its orbit (CfLightOrbit), in place:
+// per step x' = c*x - s*z, z' = s*x + c*z (products, then the difference or
+// sum, each rounded to nearest), then position = center + (x', 0, z').  Reads
+// 32 bytes and writes 32 bytes per light.
+__global__ void __launch_bounds__(256) orbit_kernel(CfLightData* __restrict__ lights,
+                                                    CfLightOrbit* __restrict__ orbits, uint64_t n, uint32_t frames)
+{
+    for (uint64_t i = blockIdx.x * 256ull + threadIdx.x; i < n; i += (uint64_t)gridDim.x * 256ull) {
+        float4* o = reinterpret_cast<float4*>(&orbits[i]);
+        float4 st = o[0];
+        const float4 ctr = o[1];
+        float x = st.x, z = st.y;
+        for (uint32_t f = 0; f < frames; ++f) {
+            const float nx = __fsub_rn(__fmul_rn(st.z, x), __fmul_rn(st.w, z));
+            const float nz = __fadd_rn(__fmul_rn(st.w, x), __fmul_rn(st.z, z));
+            x = nx;
+            z = nz;
+        }
+        st.x = x;
+        st.y = z;
+        o[0] = st;
+        *reinterpret_cast<float4*>(&lights[i].position[0]) =
+            make_float4(__fadd_rn(ctr.x, x), ctr.y, __fadd_rn(ctr.z, z), ctr.w);
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_jitter(const CfLightData* src, CfLightData* dst, uint32_t n, uint64_t seed, float sigma,
@@ -1143,6 +1185,23 @@ cudaError_t launch_jitter(const CfLightData* src, CfLightData* dst, uint32_t n, 
 {
     if (n == 0) return cudaSuccess;
     jitter_kernel<<<(n + 255) / 256, 256, 0, stream>>>(src, dst, n, seed, sigma);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_orbits(CfLightData* lights, CfLightOrbit* orbits, uint64_t n, uint32_t frames, cudaStream_t stream)
+{
+    if (n == 0) return cudaSuccess;
+    // grid-stride: at most 16 resident 256-thread blocks on each of 152 SMs
+    const uint64_t blocks = std::min<uint64_t>((n + 255) / 256, 152ull * 16ull);
+    orbit_kernel<<<(unsigned)blocks, 256, 0, stream>>>(lights, orbits, n, frames);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_aabb(const AabbJob* jobs, const uint32_t* prefix, uint32_t n_views, uint32_t blocks,
+                              cudaStream_t stream)
+{
+    if (blocks == 0) return cudaSuccess;
+    batch_aabb_kernel<<<blocks, 256, 0, stream>>>(jobs, prefix, n_views);
     return cudaGetLastError();
 }
 

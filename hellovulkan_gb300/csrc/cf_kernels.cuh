@@ -130,6 +130,18 @@ cudaError_t launch_finalize(const ViewCull& v, cudaStream_t stream);
 // dst = src with positions moved by sigma * (Irwin-Hall variate) from (seed, light, axis).
 cudaError_t launch_jitter(const CfLightData* src, CfLightData* dst, uint32_t n, uint64_t seed, float sigma,
                           cudaStream_t stream);
+// Every light `frames` steps along its orbit, in place (CfLightOrbit).
+cudaError_t launch_orbits(CfLightData* lights, CfLightOrbit* orbits, uint64_t n, uint32_t frames, cudaStream_t stream);
+
+// AABBs of many views in one launch: view v owns blocks [prefix[v], prefix[v+1])
+// of 256 clusters each.
+struct AabbJob {
+    CfClusterForwardUBO ubo;
+    CfAABB* out;
+    uint64_t _pad;
+};
+cudaError_t launch_batch_aabb(const AabbJob* jobs, const uint32_t* prefix, uint32_t n_views, uint32_t blocks,
+                              cudaStream_t stream);
 
 // Batches: every stage of many views in one launch (the culling stage once per
 // shape bucket).  `prefix` arrays hold, per view, the first block of that view

@@ -711,6 +711,16 @@ int cf_generate_aabbs(const CfClusterForwardUBO* ubo, CfAABB* d_aabbs, void* str
     return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "AABB generator launch");
 }
 
+int cf_animate_light_orbits(CfLightData* d_lights, CfLightOrbit* d_orbits, uint64_t count, uint32_t frames,
+                            void* stream)
+{
+    if (count && (!d_lights || !d_orbits)) return fail(CF_ERROR_INVALID_ARGUMENT, "cf_animate_light_orbits: null argument");
+    if ((reinterpret_cast<uintptr_t>(d_lights) | reinterpret_cast<uintptr_t>(d_orbits)) & 15)
+        return fail(CF_ERROR_INVALID_ARGUMENT, "cf_animate_light_orbits: buffers must be 16-byte aligned");
+    const cudaError_t e = cfk::launch_orbits(d_lights, d_orbits, count, frames, (cudaStream_t)stream);
+    return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "light orbit launch");
+}
+
 int cf_cull_lights(const CfClusterForwardUBO* ubo, const CfAABB* d_aabbs, const CfLightData* d_lights,
                    uint32_t light_count, uint32_t cap, CfLightCell* d_cells, uint32_t* d_indices,
                    uint64_t index_capacity, uint32_t* d_total, void* d_workspace, uint64_t workspace_bytes,

@@ -80,7 +80,9 @@ extern "C" int cf_serve_run_load(CfServer* server, const CfServeLoad* load, CfSe
     std::vector<double> arrival;
     for (double t = gap(rng); t < load->duration_s; t += gap(rng)) arrival.push_back(t);
     const size_t n = arrival.size();
-    std::vector<double> submit_lag(n, 0.0), latency(n, -1.0), queue(n, -1.0);
+    std::vector<double> submit_lag(n, 0.0), latency(n, -1.0), queue(n, -1.0), exec(n, -1.0);
+    std::vector<double> set_call(n, -1.0), submit_call(n, -1.0);  // seconds in the set call / in submit
+    std::vector<char> reused_set(n, 0);
     std::vector<uint64_t> tests(n, 0);
     std::vector<int> status(n, 0);
     std::atomic<size_t> submitted{0}, new_sets{0}, reused{0}, submit_errors{0};
@@ -98,7 +100,9 @@ extern "C" int cf_serve_run_load(CfServer* server, const CfServeLoad* load, CfSe
             uint64_t set_id = 0;
             uint32_t count = 0;
             int st = CF_SUCCESS;
+            const clk::time_point t_call = clk::now();
             if (!recent.empty() && U(r) < load->p_reuse) {
+                reused_set[i] = 1;
                 const auto& pick = recent[(size_t)(U(r) * (double)recent.size()) % recent.size()];
                 set_id = pick.first;
                 count = pick.second;
@@ -118,6 +122,7 @@ extern "C" int cf_serve_run_load(CfServer* server, const CfServeLoad* load, CfSe
                 }
                 new_sets++;
             }
+            set_call[i] = std::chrono::duration<double>(clk::now() - t_call).count();
             CfServerRequest q{};
             const uint32_t p = (uint32_t)(U(r) * load->n_projections) % load->n_projections;
             q.ubo = load->projections[p];
@@ -133,7 +138,10 @@ extern "C" int cf_serve_run_load(CfServer* server, const CfServeLoad* load, CfSe
             submit_lag[i] = secs(clk::now()) - secs(due);
             tests[i] = (uint64_t)q.ubo.sliceCountX * q.ubo.sliceCountY * q.ubo.sliceCountZ * count;
             uint64_t rid = 0;
-            if (st != CF_SUCCESS || cf_server_submit(server, &q, &rid) != CF_SUCCESS) {
+            const clk::time_point t_sub = clk::now();
+            if (st == CF_SUCCESS) st = cf_server_submit(server, &q, &rid);
+            submit_call[i] = std::chrono::duration<double>(clk::now() - t_sub).count();
+            if (st != CF_SUCCESS) {
                 submit_errors++;
                 status[i] = -1;
                 continue;
@@ -157,6 +165,7 @@ extern "C" int cf_serve_run_load(CfServer* server, const CfServeLoad* load, CfSe
                     cf_server_release(server, c.request_id);
                     latency[i] = submit_lag[i] + (c.t_complete - c.t_submit);
                     queue[i] = submit_lag[i] + (c.t_launch - c.t_submit);
+                    exec[i] = c.t_complete - c.t_launch;
                     completed++;
                 } else {
                     status[i] = c.status;
@@ -175,15 +184,18 @@ extern "C" int cf_serve_run_load(CfServer* server, const CfServeLoad* load, CfSe
     submitting_done = true;
     poll_thread.join();
 
-    std::vector<double> lat, q, lag;
+    std::vector<double> lat, q, lag, ex, reg_us, jit_us, sub_us;
     uint64_t tests_done = 0;
     for (size_t i = 0; i < n; ++i) {
         if (latency[i] >= 0) {
             lat.push_back(latency[i] * 1e3);
             q.push_back(queue[i] * 1e3);
+            ex.push_back(exec[i] * 1e3);
             tests_done += tests[i];
         }
         lag.push_back(submit_lag[i] * 1e3);
+        if (set_call[i] >= 0) (reused_set[i] ? jit_us : reg_us).push_back(set_call[i] * 1e6);
+        if (submit_call[i] >= 0) sub_us.push_back(submit_call[i] * 1e6);
     }
     const double wall = std::max(1e-9, last_done - secs(start));
     CfServeReport rep{};
@@ -204,6 +216,14 @@ extern "C" int cf_serve_run_load(CfServer* server, const CfServeLoad* load, CfSe
     rep.queue_p50_ms = percentile(q, 0.50);
     rep.queue_p99_ms = percentile(q, 0.99);
     rep.submit_lag_p99_ms = percentile(lag, 0.99);
+    rep.exec_p50_ms = percentile(ex, 0.50);
+    rep.exec_p99_ms = percentile(ex, 0.99);
+    rep.register_call_p50_us = percentile(reg_us, 0.50);
+    rep.register_call_p99_us = percentile(reg_us, 0.99);
+    rep.jitter_call_p50_us = percentile(jit_us, 0.50);
+    rep.jitter_call_p99_us = percentile(jit_us, 0.99);
+    rep.submit_call_p50_us = percentile(sub_us, 0.50);
+    rep.submit_call_p99_us = percentile(sub_us, 0.99);
     rep.tests_brute_force = tests_done;
     *report = rep;
     return CF_SUCCESS;

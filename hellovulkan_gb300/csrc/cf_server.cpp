@@ -49,13 +49,18 @@ double now_s()
     return duration<double>(steady_clock::now().time_since_epoch()).count();
 }
 
+// One version of a light set.  Every fill (host upload or jitter) is
+// enqueued on the server's single upload stream, so fills run in the order
+// they were enqueued, and a batch orders itself after all of them by waiting
+// on a fence recorded on the upload stream when it is launched.  A version's
+// memory may therefore go back to the arena as soon as no admitted request
+// references it: a later fill reuses it behind the earlier ones on the same
+// stream, and a later batch reuses it behind its fence.
 struct LightVersion {
     unsigned char* d = nullptr;
     uint32_t count = 0;
     uint32_t refs = 0;
     bool retired = false;
-    cudaEvent_t ready = nullptr;      // the upload (or jitter) that fills it
-    cudaEvent_t last_read = nullptr;  // the last jitter that reads it, if any
 };
 
 struct LightSet {
@@ -67,7 +72,8 @@ struct AabbEntry {
     CfClusterForwardUBO key{};
     unsigned char* d = nullptr;
     uint32_t refs = 0;
-    bool generated = false;
+    bool generated = false;  // its generation has been enqueued
+    bool complete = false;   // a batch that used it has finished, so it is in memory
     cudaEvent_t ready = nullptr;
     uint64_t last_use = 0;
 };
@@ -80,7 +86,7 @@ struct Request {
     AabbEntry* aabb = nullptr;
     unsigned char* ws = nullptr;
     unsigned char* out = nullptr;
-    uint32_t clusters = 0;
+    uint32_t clusters = 0, groups = 0;
     cfk::CullConfig cfg{};
     cfk::WorkspaceLayout layout{};
     int status = CF_SUCCESS;
@@ -88,16 +94,45 @@ struct Request {
 
 struct Batch;
 
+// The tables of one batch, in one pinned host block mirrored by one device
+// block so that they go over in a single copy: the ViewJob records, the three
+// block-prefix arrays, then the (view, group) work items, each section
+// 256-byte aligned.
+struct TableLayout {
+    size_t jobs = 0, prefix = 0, items = 0, bytes = 0;
+};
+
+TableLayout table_layout(uint32_t views, uint32_t items)
+{
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    TableLayout t;
+    t.prefix = al((size_t)views * sizeof(cfk::ViewJob));
+    t.items = t.prefix + al((size_t)views * 3 * sizeof(uint32_t));
+    t.bytes = t.items + al((size_t)items * sizeof(uint2));
+    return t;
+}
+
 struct StreamSlot {
     cudaStream_t s = nullptr;
     bool busy = false;
-    cfk::ViewJob* d_jobs = nullptr;
-    uint32_t* d_prefix = nullptr;
-    uint2* d_items = nullptr;
+    unsigned char* d_tables = nullptr;
+    unsigned char* h_tables = nullptr;
     uint32_t* d_queues = nullptr;
-    cfk::ViewJob* h_jobs = nullptr;
-    uint32_t* h_prefix = nullptr;
-    uint2* h_items = nullptr;
+    cudaEvent_t upload_fence = nullptr;  // recorded on the upload stream at each launch
+};
+
+// What a launch needs once the tables are written (everything but the CUDA
+// calls is done with the server lock held; the calls themselves are not).
+struct LaunchPlan {
+    struct Bucket {
+        cfk::CullConfig cfg;
+        uint32_t begin, count;
+    };
+    std::vector<Bucket> buckets;
+    std::vector<AabbEntry*> generate;  // AABBs this batch generates
+    std::vector<AabbEntry*> wait;      // AABBs generated by batches that may still run
+    TableLayout tables;
+    uint32_t views = 0, items = 0, xform_blocks = 0, bin_blocks = 0, copy_blocks = 0;
 };
 
 struct Batch {
@@ -148,7 +183,6 @@ struct CfServer {
     std::deque<Batch*> finished;
     std::atomic<uint32_t> finished_n{0};
     std::map<uint32_t, cfk::CullConfig> tuned;
-    std::vector<std::pair<unsigned char*, cudaEvent_t>> deferred;  // freed once the event has completed
     std::thread worker;
     bool stop = false;
     cudaStream_t upload = nullptr;
@@ -171,25 +205,9 @@ cfk::CullConfig server_config_for(const CfServer* s, uint32_t xy)
 void free_version_if_dead(CfServer* s, LightVersion* v)
 {
     if (v && v->retired && v->refs == 0) {
-        if (v->last_read) s->deferred.emplace_back(v->d, v->last_read);  // a jitter may still read it
-        else s->arena.release(v->d);
-        if (v->ready) cudaEventDestroy(v->ready);
+        s->arena.release(v->d);
         delete v;
     }
-}
-
-void reap_deferred(CfServer* s)
-{
-    auto keep = s->deferred.begin();
-    for (auto it = s->deferred.begin(); it != s->deferred.end(); ++it) {
-        if (cudaEventQuery(it->second) == cudaSuccess) {
-            s->arena.release(it->first);
-            cudaEventDestroy(it->second);
-        } else {
-            *keep++ = *it;
-        }
-    }
-    s->deferred.erase(keep, s->deferred.end());
 }
 
 // Frees the least recently used light set or AABB entry nobody in flight
@@ -234,7 +252,6 @@ bool evict_one(CfServer* s)
 
 unsigned char* arena_alloc(CfServer* s, size_t bytes)
 {
-    reap_deferred(s);
     for (;;) {
         unsigned char* p = s->arena.alloc(bytes);
         if (p) {
@@ -284,6 +301,7 @@ bool admit(CfServer* s, Request* r)
         r->status = CF_ERROR_CAPACITY;
         return true;
     }
+    r->groups = groups;
     r->layout = cfk::workspace_layout(r->clusters, lv->count, r->req.max_lights_per_cluster, Z, true, groups);
     AabbEntry* a = nullptr;
     for (AabbEntry* e : s->aabbs)
@@ -295,6 +313,11 @@ bool admit(CfServer* s, Request* r)
         a = new AabbEntry();
         a->key = u;
         a->d = arena_alloc(s, (size_t)r->clusters * sizeof(CfAABB));
+        if (a->d && cudaEventCreateWithFlags(&a->ready, cudaEventDisableTiming) != cudaSuccess) {
+            s->arena.release(a->d);
+            a->d = nullptr;
+            a->ready = nullptr;
+        }
         if (!a->d) {
             delete a;
             return false;
@@ -311,6 +334,7 @@ bool admit(CfServer* s, Request* r)
         a->refs--;
         if (new_aabb) {
             s->arena.release(a->d);
+            cudaEventDestroy(a->ready);
             s->aabbs.erase(std::find(s->aabbs.begin(), s->aabbs.end(), a));
             delete a;
         }
@@ -344,35 +368,38 @@ void take_finished(CfServer* s, std::deque<Batch*>& out)
     s->finished_n.fetch_sub((uint32_t)out.size());
 }
 
-int launch_batch(CfServer* s, int slot_i, std::vector<Request*>& reqs)
+// Writes the batch's tables into the slot's pinned block and decides which
+// AABBs it generates or waits for (server lock held).
+void plan_batch(CfServer* s, int slot_i, const std::vector<Request*>& reqs, LaunchPlan& plan)
 {
     StreamSlot& sl = s->slots[slot_i];
     const uint32_t n = (uint32_t)reqs.size();
-    cudaStream_t st = sl.s;
-    cudaError_t e = cudaSuccess;
-    // inputs produced elsewhere: light uploads and AABBs generated by other batches
+    plan = LaunchPlan{};
+    plan.views = n;
     for (Request* r : reqs) {
-        if (r->lights->ready) e = cudaStreamWaitEvent(st, r->lights->ready, 0);
-        if (e != cudaSuccess) return cuda_fail(e, "wait for light upload");
         AabbEntry* a = r->aabb;
         if (!a->generated) {
-            e = cfk::launch_aabb(r->req.ubo, reinterpret_cast<CfAABB*>(a->d), st);
-            if (e == cudaSuccess && !a->ready) e = cudaEventCreateWithFlags(&a->ready, cudaEventDisableTiming);
-            if (e == cudaSuccess) e = cudaEventRecord(a->ready, st);
-            if (e != cudaSuccess) return cuda_fail(e, "AABB generation");
             a->generated = true;
-        } else if (a->ready) {
-            e = cudaStreamWaitEvent(st, a->ready, 0);
-            if (e != cudaSuccess) return cuda_fail(e, "wait for AABBs");
+            plan.generate.push_back(a);
+        } else if (!a->complete && std::find(plan.wait.begin(), plan.wait.end(), a) == plan.wait.end() &&
+                   std::find(plan.generate.begin(), plan.generate.end(), a) == plan.generate.end()) {
+            plan.wait.push_back(a);
         }
     }
-    // tables
+    // items are counted first: their section follows the jobs and prefixes
+    uint32_t items = 0;
+    for (Request* r : reqs) items += r->groups;
+    plan.items = items;
+    plan.tables = table_layout(n, items);
+    cfk::ViewJob* jobs = reinterpret_cast<cfk::ViewJob*>(sl.h_tables);
+    uint32_t* prefix = reinterpret_cast<uint32_t*>(sl.h_tables + plan.tables.prefix);
+    uint2* it = reinterpret_cast<uint2*>(sl.h_tables + plan.tables.items);
     std::map<uint32_t, std::vector<uint32_t>> buckets;
     uint32_t xb = 0, bb = 0, cb = 0;
     for (uint32_t i = 0; i < n; ++i) {
         Request* r = reqs[i];
         const CfClusterForwardUBO& u = r->req.ubo;
-        cfk::ViewJob& j = sl.h_jobs[i];
+        cfk::ViewJob& j = jobs[i];
         j = cfk::ViewJob{};
         const cfk::WorkspaceLayout& L = r->layout;
         unsigned char* w = r->ws;
@@ -399,63 +426,85 @@ int launch_batch(CfServer* s, int slot_i, std::vector<Request*>& reqs)
         j.v.slice_clusters = u.sliceCountX * u.sliceCountY;
         j.v.slices = u.sliceCountZ;
         j.v.group_width = (uint32_t)(r->cfg.warps * r->cfg.clusters_per_warp);
-        j.v.groups = cfk::group_count(r->clusters, j.v.slice_clusters, j.v.slices, j.v.group_width, true);
+        j.v.groups = r->groups;
         j.v.binned = 1;
         j.lights = reinterpret_cast<const CfLightData*>(r->lights->d);
         j.light_count = r->lights->count;
         for (int q = 0; q < 16; ++q) j.view[q] = u.cameraView[q];
-        sl.h_prefix[i] = xb;
-        sl.h_prefix[n + i] = bb;
-        sl.h_prefix[2 * n + i] = cb;
+        prefix[i] = xb;
+        prefix[n + i] = bb;
+        prefix[2 * n + i] = cb;
         xb += cfk::granules(j.v.lpad);
         bb += j.v.slices;
         cb += cfk::copy_blocks(r->clusters);
         buckets[j.v.slice_clusters].push_back(i);
     }
-    struct B {
-        cfk::CullConfig cfg;
-        uint32_t begin, count;
-    };
-    std::vector<B> bl;
     uint32_t ni = 0;
     for (auto& kv : buckets) {
-        B bk{reqs[kv.second[0]]->cfg, ni, 0};
+        LaunchPlan::Bucket bk{reqs[kv.second[0]]->cfg, ni, 0};
         for (uint32_t vi : kv.second)
-            for (uint32_t g = 0; g < sl.h_jobs[vi].v.groups; ++g) sl.h_items[ni++] = make_uint2(vi, g);
+            for (uint32_t g = 0; g < jobs[vi].v.groups; ++g) it[ni++] = make_uint2(vi, g);
         bk.count = ni - bk.begin;
-        bl.push_back(bk);
+        plan.buckets.push_back(bk);
     }
-    e = cudaMemcpyAsync(sl.d_jobs, sl.h_jobs, n * sizeof(cfk::ViewJob), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(sl.d_prefix, sl.h_prefix, 3 * n * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess && ni) e = cudaMemcpyAsync(sl.d_items, sl.h_items, ni * sizeof(uint2), cudaMemcpyHostToDevice, st);
+    plan.xform_blocks = xb;
+    plan.bin_blocks = bb;
+    plan.copy_blocks = cb;
+}
+
+// Enqueues a planned batch on its slot's stream (server lock NOT held: only
+// the worker thread launches, and the slot, the requests and their memory are
+// its own until the batch's host callback runs).
+int enqueue_batch(CfServer* s, int slot_i, const LaunchPlan& plan, const std::vector<Request*>& reqs)
+{
+    StreamSlot& sl = s->slots[slot_i];
+    cudaStream_t st = sl.s;
+    const uint32_t n = plan.views;
+    // every fill enqueued so far (the versions these requests bound, and any
+    // reader of memory they were given) before this batch's first kernel
+    cudaError_t e = cudaEventRecord(sl.upload_fence, s->upload);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, sl.upload_fence, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "upload fence");
+    for (AabbEntry* a : plan.generate) {
+        const Request* r = *std::find_if(reqs.begin(), reqs.end(), [a](const Request* q) { return q->aabb == a; });
+        e = cfk::launch_aabb(r->req.ubo, reinterpret_cast<CfAABB*>(a->d), st);
+        if (e == cudaSuccess) e = cudaEventRecord(a->ready, st);
+        if (e != cudaSuccess) return cuda_fail(e, "AABB generation");
+    }
+    for (AabbEntry* a : plan.wait) {
+        e = cudaStreamWaitEvent(st, a->ready, 0);
+        if (e != cudaSuccess) return cuda_fail(e, "wait for AABBs");
+    }
+    cfk::ViewJob* d_jobs = reinterpret_cast<cfk::ViewJob*>(sl.d_tables);
+    const uint32_t* d_prefix = reinterpret_cast<const uint32_t*>(sl.d_tables + plan.tables.prefix);
+    const uint2* d_items = reinterpret_cast<const uint2*>(sl.d_tables + plan.tables.items);
+    e = cudaMemcpyAsync(sl.d_tables, sl.h_tables, plan.tables.items + (size_t)plan.items * sizeof(uint2),
+                        cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
-        e = cfk::launch_batch_xform(sl.d_jobs, sl.d_prefix, n, xb, sl.d_queues, (uint32_t)bl.size(), st);
-    if (e == cudaSuccess) e = cfk::launch_batch_bin(sl.d_jobs, sl.d_prefix + n, n, bb, st);
-    for (size_t q = 0; q < bl.size() && e == cudaSuccess; ++q) {
+        e = cfk::launch_batch_xform(d_jobs, d_prefix, n, plan.xform_blocks, sl.d_queues,
+                                    (uint32_t)plan.buckets.size(), st);
+    if (e == cudaSuccess) e = cfk::launch_batch_bin(d_jobs, d_prefix + n, n, plan.bin_blocks, st);
+    for (size_t q = 0; q < plan.buckets.size() && e == cudaSuccess; ++q) {
+        const LaunchPlan::Bucket& bk = plan.buckets[q];
         int ctas = 0;
-        e = cfk::batch_cull_resident_ctas(bl[q].cfg, &ctas);
+        e = cfk::batch_cull_resident_ctas(bk.cfg, &ctas);
         if (e != cudaSuccess) break;
-        cfk::BatchCull bc{sl.d_jobs, sl.d_items + bl[q].begin, bl[q].count, sl.d_queues + q};
-        e = cfk::launch_batch_cull(bc, bl[q].cfg, std::min<int>(ctas, (int)bl[q].count), s->dev_error, st);
+        cfk::BatchCull bc{d_jobs, d_items + bk.begin, bk.count, sl.d_queues + q};
+        e = cfk::launch_batch_cull(bc, bk.cfg, std::min<int>(ctas, (int)bk.count), s->dev_error, st);
     }
-    if (e == cudaSuccess) e = cfk::launch_batch_scan(sl.d_jobs, n, st);
-    if (e == cudaSuccess) e = cfk::launch_batch_copy(sl.d_jobs, sl.d_prefix + 2 * n, n, cb, st);
+    if (e == cudaSuccess) e = cfk::launch_batch_scan(d_jobs, n, st);
+    if (e == cudaSuccess) e = cfk::launch_batch_copy(d_jobs, d_prefix + 2 * n, n, plan.copy_blocks, st);
     if (e != cudaSuccess) return cuda_fail(e, "server batch launch");
-    Batch* b = new Batch();
+    Batch* b = new (std::nothrow) Batch();
+    if (!b) return fail(CF_ERROR_OUT_OF_MEMORY, "host allocation");
     b->server = s;
     b->slot = slot_i;
     b->reqs = reqs;
-    const double t = now_s();
-    for (Request* r : reqs) r->t_launch = t;
     e = cudaLaunchHostFunc(st, on_batch_done, b);
     if (e != cudaSuccess) {
         delete b;
         return cuda_fail(e, "cudaLaunchHostFunc");
     }
-    sl.busy = true;
-    s->stats.batches++;
-    s->stats.views_launched += n;
-    s->stats.max_batch_views = std::max<uint32_t>(s->stats.max_batch_views, n);
     return CF_SUCCESS;
 }
 
@@ -467,6 +516,7 @@ void finish_batch(CfServer* s, Batch* b)
         r->lights->refs--;
         free_version_if_dead(s, r->lights);
         r->aabb->refs--;
+        r->aabb->complete = true;  // this batch waited for (or made) it and has finished
         s->arena.release(r->ws);
         r->ws = nullptr;
         complete_request(s, r, CF_SUCCESS);
@@ -522,8 +572,19 @@ void worker_main(CfServer* s)
                 }
                 break;
             }
-            const int st = launch_batch(s, (int)q, batch);
+            LaunchPlan plan;
+            plan_batch(s, (int)q, batch, plan);
+            s->slots[q].busy = true;
+            const double t_launch = now_s();
+            for (Request* r : batch) r->t_launch = t_launch;
+            // The CUDA calls go without the lock, so that submitters, pollers
+            // and uploads are not held up behind them.
+            lk.unlock();
+            const int st = enqueue_batch(s, (int)q, plan, batch);
+            lk.lock();
             if (st != CF_SUCCESS) {
+                s->slots[q].busy = false;
+                for (AabbEntry* a : plan.generate) a->generated = false;
                 for (Request* r : batch) {
                     r->lights->refs--;
                     free_version_if_dead(s, r->lights);
@@ -533,6 +594,9 @@ void worker_main(CfServer* s)
                     complete_request(s, r, st);
                 }
             } else {
+                s->stats.batches++;
+                s->stats.views_launched += batch.size();
+                s->stats.max_batch_views = std::max<uint32_t>(s->stats.max_batch_views, (uint32_t)batch.size());
                 launched = true;
             }
         }
@@ -569,17 +633,15 @@ int upload_version(CfServer* s, const CfLightData* host, uint32_t n, LightVersio
 int fill_from_host(CfServer* s, LightVersion* v, const CfLightData* host)
 {
     DeviceGuard g(s->device);
-    cudaError_t e = cudaEventCreateWithFlags(&v->ready, cudaEventDisableTiming);
-    if (e == cudaSuccess && v->count)
+    cudaError_t e = cudaSuccess;
+    if (v->count)
         e = cudaMemcpyAsync(v->d, host, (size_t)v->count * sizeof(CfLightData), cudaMemcpyHostToDevice, s->upload);
-    if (e == cudaSuccess) e = cudaEventRecord(v->ready, s->upload);
     return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "light set upload");
 }
 
 void drop_unpublished(CfServer* s, LightVersion* v)
 {
     s->arena.release(v->d);
-    if (v->ready) cudaEventDestroy(v->ready);
     delete v;
     s->memory_epoch++;
 }
@@ -587,13 +649,10 @@ void drop_unpublished(CfServer* s, LightVersion* v)
 void destroy_slot(StreamSlot& sl)
 {
     if (sl.s) cudaStreamDestroy(sl.s);
-    cudaFree(sl.d_jobs);
-    cudaFree(sl.d_prefix);
-    cudaFree(sl.d_items);
+    if (sl.upload_fence) cudaEventDestroy(sl.upload_fence);
+    cudaFree(sl.d_tables);
     cudaFree(sl.d_queues);
-    cudaFreeHost(sl.h_jobs);
-    cudaFreeHost(sl.h_prefix);
-    cudaFreeHost(sl.h_items);
+    cudaFreeHost(sl.h_tables);
 }
 
 }  // namespace
@@ -626,13 +685,11 @@ int cf_server_create(CfContext* ctx, const CfServerConfig* config, CfServer** ou
     s->slots.resize(c.streams);
     for (StreamSlot& sl : s->slots) {
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.s, cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaMalloc(&sl.d_jobs, c.max_batch_views * sizeof(cfk::ViewJob));
-        if (e == cudaSuccess) e = cudaMalloc(&sl.d_prefix, 3 * c.max_batch_views * sizeof(uint32_t));
-        if (e == cudaSuccess) e = cudaMalloc(&sl.d_items, (size_t)s->items_per_slot * sizeof(uint2));
+        const size_t tb = table_layout(c.max_batch_views, s->items_per_slot).bytes;
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.upload_fence, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_tables, tb);
         if (e == cudaSuccess) e = cudaMalloc(&sl.d_queues, cfk::kMaxBatchQueues * sizeof(uint32_t));
-        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_jobs, c.max_batch_views * sizeof(cfk::ViewJob));
-        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_prefix, 3 * c.max_batch_views * sizeof(uint32_t));
-        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_items, (size_t)s->items_per_slot * sizeof(uint2));
+        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_tables, tb);
     }
     if (e != cudaSuccess) {
         for (StreamSlot& sl : s->slots) destroy_slot(sl);
@@ -658,12 +715,8 @@ int cf_server_destroy(CfServer* s)
     if (s->worker.joinable()) s->worker.join();
     DeviceGuard g(s->device);
     cudaDeviceSynchronize();
-    for (auto& d : s->deferred) cudaEventDestroy(d.second);
     for (auto& kv : s->holding) delete kv.second;
-    for (auto& kv : s->sets) {
-        if (kv.second.cur->ready) cudaEventDestroy(kv.second.cur->ready);
-        delete kv.second.cur;
-    }
+    for (auto& kv : s->sets) delete kv.second.cur;
     for (AabbEntry* a : s->aabbs) {
         if (a->ready) cudaEventDestroy(a->ready);
         delete a;
@@ -705,7 +758,7 @@ int publish_version(CfServer* s, uint64_t id, LightVersion* v, LightVersion* pin
     auto it = s->sets.find(id);
     if (it == s->sets.end()) {
         free_version_if_dead(s, pinned_old);
-        s->deferred.emplace_back(v->d, v->ready);  // its fill may still be running
+        s->arena.release(v->d);  // its fill may still run: later users order after it (see LightVersion)
         delete v;
         return fail(CF_ERROR_NOT_READY, "light set %llu was released", (unsigned long long)id);
     }
@@ -764,18 +817,14 @@ int cf_server_jitter_light_set(CfServer* s, uint64_t id, uint64_t seed, float si
         }
         v->d = d;
         v->count = old->count;
-        if (!old->last_read) cudaEventCreateWithFlags(&old->last_read, cudaEventDisableTiming);
     }
     cudaError_t e;
     {
-        DeviceGuard g(s->device);  // not under `mu`
-        e = cudaEventCreateWithFlags(&v->ready, cudaEventDisableTiming);
-        if (e == cudaSuccess && old->ready) e = cudaStreamWaitEvent(s->upload, old->ready, 0);
-        if (e == cudaSuccess)
-            e = cfk::launch_jitter(reinterpret_cast<const CfLightData*>(old->d), reinterpret_cast<CfLightData*>(v->d),
-                                   old->count, seed, sigma, s->upload);
-        if (e == cudaSuccess) e = cudaEventRecord(v->ready, s->upload);
-        if (e == cudaSuccess && old->last_read) e = cudaEventRecord(old->last_read, s->upload);
+        // Not under `mu`.  The fill of `old` was enqueued on the upload stream
+        // before `old` was published, so this jitter runs after it.
+        DeviceGuard g(s->device);
+        e = cfk::launch_jitter(reinterpret_cast<const CfLightData*>(old->d), reinterpret_cast<CfLightData*>(v->d),
+                               old->count, seed, sigma, s->upload);
     }
     std::lock_guard<std::mutex> lk(s->mu);
     if (e != cudaSuccess) {

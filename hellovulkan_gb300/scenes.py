@@ -20,6 +20,14 @@ configurations.
                  uniform in [-80,80]x[2,40]x[-80,80] looking at a uniform
                  target in [-20,20]^3; near 0.1, far 2000
 
+  stress         n_views views x n_lights lights each (4096 x 4096 at full
+                 size), lights drawn like plain_large around per-view blobs and
+                 moving on horizontal circles of radius U[1,10] at angular speed
+                 U[0.1,2] rad/s, 60 frames per second; the projection changes
+                 every 60 frames: view i uses grid STRESS_GRIDS[(i + epoch) % 2]
+                 (16x9x24 at 1920x1080, 32x18x48 at 2560x1440) and fovY
+                 alternates 45 / 60 degrees; cameras as batch_mix
+
 LightData records are numpy float32 arrays of shape (n, 12): position xyzw,
 color rgba, radius, 3 pad words (the 48-byte std430 record).
 """
@@ -132,3 +140,55 @@ def custom_view(grid, width, height, near, far, view=None, lights=None, cap=CAP,
     ubo = cluster_forward_ubo(fovy, width, height, near, far, view, grid)
     lights = np.zeros((0, 12), np.float32) if lights is None else lights
     return View(ubo, lights, cap, "custom")
+
+
+STRESS_GRIDS = ((16, 9, 24), (32, 18, 48))
+STRESS_FPS = 60.0
+
+
+def orbit_lights(rng: np.random.Generator, n_views: int, n_lights: int, n_blobs: int = 32, sigma: float = 8.0):
+    """(lights (n_views * n_lights, 12), orbits (n_views * n_lights, 8)) float32:
+    each view's lights around its own 32 Gaussian blobs, each light on a
+    horizontal circle (CfLightOrbit: offset x/z, cos/sin of the angle per frame,
+    centre xyz + position w).  Positions are centre + offset, rounded to float32
+    like the device does."""
+    centres = np.stack([rng.uniform(-100, 100, (n_views, n_blobs)), rng.uniform(0, 30, (n_views, n_blobs)),
+                        rng.uniform(-100, 100, (n_views, n_blobs))], axis=2)
+    which = rng.integers(0, n_blobs, size=(n_views, n_lights))
+    centre = np.take_along_axis(centres, which[..., None], axis=1).reshape(-1, 3)
+    centre = (centre + rng.normal(0.0, sigma, size=centre.shape)).astype(np.float32)
+    n = n_views * n_lights
+    radius = np.clip(rng.lognormal(math.log(3.0), 0.5, size=n), 0.5, 20.0).astype(np.float32)
+    color = rng.uniform(0.0, 1.0, size=(n, 3)).astype(np.float32)
+    rho = rng.uniform(1.0, 10.0, n)
+    omega = rng.uniform(0.1, 2.0, n)
+    phase = rng.uniform(0.0, 2.0 * math.pi, n)
+    orbits = np.empty((n, 8), np.float32)
+    orbits[:, 0] = rho * np.cos(phase)
+    orbits[:, 1] = rho * np.sin(phase)
+    orbits[:, 2] = np.cos(omega / STRESS_FPS)
+    orbits[:, 3] = np.sin(omega / STRESS_FPS)
+    orbits[:, 4:7] = centre
+    orbits[:, 7] = 1.0
+    pos = np.empty((n, 3), np.float32)
+    pos[:, 0] = orbits[:, 4] + orbits[:, 0]
+    pos[:, 1] = orbits[:, 5]
+    pos[:, 2] = orbits[:, 6] + orbits[:, 1]
+    return make_lights(pos, radius, color), orbits
+
+
+_STRESS_PROJ = {}
+
+
+def stress_ubo(view_index: int, epoch: int, camera) -> CfClusterForwardUBO:
+    """The UBO of stress view `view_index` during projection epoch `epoch`."""
+    grid = STRESS_GRIDS[(view_index + epoch) % 2]
+    key = (grid, epoch % 2)
+    if key not in _STRESS_PROJ:  # two projections per epoch: build each once
+        t = 120 if grid == (16, 9, 24) else 80
+        fovy = math.radians(45.0 if epoch % 2 == 0 else 60.0)
+        _STRESS_PROJ[key] = bytes(cluster_forward_ubo(fovy, grid[0] * t, grid[1] * t, 0.1, 2000.0,
+                                                      np.eye(4, dtype=np.float32), grid))
+    u = CfClusterForwardUBO.from_buffer_copy(_STRESS_PROJ[key])
+    u.cameraView[:] = np.asarray(camera, np.float32).T.reshape(-1).tolist()
+    return u

@@ -62,6 +62,19 @@ typedef struct CfLightCell {
     uint32_t count;
 } CfLightCell;
 
+/* Circular motion of one light in the horizontal plane, advanced one frame
+ * at a time on the device (cf_animate_light_orbits): offset' = R * offset
+ * with R = [[cos, -sin], [sin, cos]] the rotation of one frame (omega * dt),
+ * then position = (center.x + offset.x, center.y, center.z + offset.z,
+ * center.w).  No reference counterpart: the reference's lights are static
+ * (ResourcesLight::UpdateLightPosition, Source/Resources/ResourcesLight.cpp:20-29,
+ * moves one light from the host). */
+typedef struct CfLightOrbit {
+    CF_ALIGNAS(16) float offset[2]; /* (x, z) from the centre              */
+    float rot[2];                   /* (cos, sin) of the angle per frame   */
+    float center[4];                /* x, y, z and the position's w        */
+} CfLightOrbit;
+
 /* Per-view parameters, std140: invProj @0, view @64, screenSize @128,
  * sliceScaling @136, sliceBias @140, near @144, far @148, X/Y/Z @152/156/160.
  * 164 bytes are used; the C++ mirror in the reference is 176 bytes. */
@@ -92,6 +105,7 @@ static_assert(offsetof(CfAABB, maxPoint) == 16, "AABB.maxPoint @16");
 static_assert(sizeof(CfLightCell) == 8, "LightCell is two uint");
 static_assert(offsetof(CfLightCell, count) == 4, "LightCell.count @4");
 static_assert(sizeof(CfClusterForwardUBO) == 176, "ClusterForwardUBO C++ sizeof");
+static_assert(sizeof(CfLightOrbit) == 32 && offsetof(CfLightOrbit, center) == 16, "LightOrbit is two float4");
 static_assert(offsetof(CfClusterForwardUBO, cameraView) == 64, "view @64");
 static_assert(offsetof(CfClusterForwardUBO, screenSize) == 128, "screenSize @128");
 static_assert(offsetof(CfClusterForwardUBO, sliceScaling) == 136, "sliceScaling @136");

@@ -347,6 +347,10 @@ typedef struct CfServeReport {
     double latency_p50_ms, latency_p90_ms, latency_p99_ms, latency_p999_ms, latency_max_ms; /* arrival -> done */
     double queue_p50_ms, queue_p99_ms;                                                     /* arrival -> launch */
     double submit_lag_p99_ms;                                                              /* arrival -> submit */
+    double exec_p50_ms, exec_p99_ms;                                                       /* launch -> done    */
+    double register_call_p50_us, register_call_p99_us;  /* time inside cf_server_register_light_set */
+    double jitter_call_p50_us, jitter_call_p99_us;      /* time inside cf_server_jitter_light_set   */
+    double submit_call_p50_us, submit_call_p99_us;      /* time inside cf_server_submit             */
 } CfServeReport;
 
 CFCULL_API int cf_serve_run_load(CfServer* server, const CfServeLoad* load, CfServeReport* report);
@@ -362,6 +366,14 @@ CFCULL_API int cf_cull_workspace_size(const CfClusterForwardUBO* ubo, uint32_t l
 /* AABBGenerator.comp over the grid of `ubo` (host pointer) into
  * d_aabbs[X*Y*Z] (device). */
 CFCULL_API int cf_generate_aabbs(const CfClusterForwardUBO* ubo, CfAABB* d_aabbs, void* stream);
+/* Moves d_lights[0..count) `frames` steps along their orbits d_orbits[0..count)
+ * in place (CfLightOrbit, include/cf_types.h); both device buffers, 16-byte
+ * aligned; stream-ordered, so a cull enqueued after it on the same stream sees
+ * the new positions.  The device-side counterpart of
+ * ResourcesLight::UpdateLightPosition (Source/Resources/ResourcesLight.cpp:20-29)
+ * for every light at once. */
+CFCULL_API int cf_animate_light_orbits(CfLightData* d_lights, CfLightOrbit* d_orbits, uint64_t count, uint32_t frames,
+                                       void* stream);
 /* LightCulling.comp: d_cells[C] and d_indices (capacity >= C * cap) from
  * d_aabbs[C] and d_lights[light_count]; d_total (optional, device) receives
  * the number of indices.  d_workspace: >= cf_cull_workspace_size bytes,

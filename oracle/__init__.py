@@ -142,3 +142,17 @@ def jitter_lights(lights: np.ndarray, seed: int, sigma: float) -> np.ndarray:
                 s = s + (x >> np.uint64(40)).astype(np.float32) * np.float32(2.0 ** -24)
             L[:, a] = L[:, a] + np.float32(sigma) * (s - np.float32(6.0))
     return L
+
+
+def animate_orbits(orbits: np.ndarray, frames: int):
+    """Host restatement of cf_animate_light_orbits (hellovulkan_gb300/csrc/
+    cf_kernels.cu orbit_kernel), bit for bit: returns (orbits after `frames`
+    steps, positions (n, 4)).  numpy float32 products and sums round to nearest
+    one operation at a time, as the kernel's __fmul_rn / __fadd_rn do."""
+    o = np.array(orbits, np.float32, copy=True).reshape(-1, 8)
+    x, z, c, s = o[:, 0].copy(), o[:, 1].copy(), o[:, 2], o[:, 3]
+    for _ in range(frames):
+        x, z = c * x - s * z, s * x + c * z
+    o[:, 0], o[:, 1] = x, z
+    pos = np.stack([o[:, 4] + x, o[:, 5], o[:, 6] + z, o[:, 7]], axis=1).astype(np.float32)
+    return o, pos

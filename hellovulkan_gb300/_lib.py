@@ -33,6 +33,16 @@ class CfLightOrbit(C.Structure):
     _fields_ = [("offset", C.c_float * 2), ("rot", C.c_float * 2), ("center", C.c_float * 4)]
 
 
+class CfFragmentSample(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in ("cluster", "offset", "count", "covering", "missing", "flags")] + [
+        ("view_z", C.c_float), ("linear_depth", C.c_float)]
+
+
+FRAGMENT_DTYPE = np.dtype([("cluster", "<u4"), ("offset", "<u4"), ("count", "<u4"), ("covering", "<u4"),
+                           ("missing", "<u4"), ("flags", "<u4"), ("view_z", "<f4"), ("linear_depth", "<f4")])
+FRAGMENT_OUTSIDE_GRID, FRAGMENT_OUTSIDE_AABB, FRAGMENT_CAPPED, FRAGMENT_BAD_CELL = 1, 2, 4, 8
+
+
 class CfClusterForwardUBO(C.Structure):
     _fields_ = [
         ("cameraInverseProjection", C.c_float * 16),
@@ -136,7 +146,7 @@ assert C.sizeof(CfServeLoad) == 128 and C.sizeof(CfServeReport) == 208
 assert CfServeLoad.projections.offset == 56 and CfServeLoad.eye_lo.offset == 80
 assert C.sizeof(CfBatchView) == 240 and C.sizeof(CfBatchInfo) == 216
 assert C.sizeof(CfLightData) == 48 and C.sizeof(CfAABB) == 32 and C.sizeof(CfLightCell) == 8
-assert C.sizeof(CfLightOrbit) == 32
+assert C.sizeof(CfLightOrbit) == 32 and C.sizeof(CfFragmentSample) == 32 == FRAGMENT_DTYPE.itemsize
 assert C.sizeof(CfClusterForwardUBO) == 176
 
 STATUS = {
@@ -198,6 +208,8 @@ _SIGS = {
     "cf_cull_workspace_size": [C.POINTER(CfClusterForwardUBO), _U32, _U32, _PU64],
     "cf_generate_aabbs": [C.POINTER(CfClusterForwardUBO), _P, _P],
     "cf_animate_light_orbits": [_P, _P, _U64, _U32, _P],
+    "cf_lookup_clusters": [C.POINTER(CfClusterForwardUBO), _P, _U32, _U32, _P, _P, _U64, _P, _U32, _U32, _P, _I, _P,
+                           _P],
     "cf_cull_lights": [C.POINTER(CfClusterForwardUBO), _P, _P, _U32, _U32, _P, _P, _U64, _P, _P, _U64, _P],
     "cf_cull_workspace_device_error": [_P, _PU32],
     "cf_cull_lights_static_scratch": [C.POINTER(CfClusterForwardUBO), _P, _P, _U32, _U32, _P, _P, _U64, _P, _P, _P],

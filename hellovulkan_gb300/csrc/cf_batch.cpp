@@ -82,9 +82,36 @@ struct CfBatch {
     bool use_graph = true;
     cudaGraphExec_t exec = nullptr;
     cudaStream_t graph_stream = nullptr;
+    // Recorded after the last pass or AABB generation enqueued outside a
+    // stream capture: the device tables, the workspace and the graph are not
+    // changed until it has completed.
+    cudaEvent_t last_use = nullptr;
+    bool used = false;
 };
 
 namespace {
+
+// Waits until no work this batch enqueued can still read its tables.
+int wait_idle(CfBatch* b)
+{
+    if (!b->used) return CF_SUCCESS;
+    const cudaError_t e = cudaEventSynchronize(b->last_use);
+    if (e != cudaSuccess) return cuda_fail(e, "waiting for the batch's last pass");
+    b->used = false;
+    return CF_SUCCESS;
+}
+
+// Notes work enqueued on st that reads the batch's tables.
+int mark_used(CfBatch* b, cudaStream_t st)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(st, &cs);
+    if (e == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
+        e = cudaEventRecord(b->last_use, st);
+        if (e == cudaSuccess) b->used = true;
+    }
+    return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "batch completion event");
+}
 
 void drop_graph(CfBatch* b)
 {
@@ -115,6 +142,8 @@ int validate_view(const CfBatchView& v, uint32_t i, uint32_t* clusters)
 // Recomputes every derived table from b->views and b->tuned and uploads it.
 int rebuild(CfBatch* b)
 {
+    const int w = wait_idle(b);  // passes still queued read the tables rewritten below
+    if (w) return w;
     drop_graph(b);
     const uint32_t n = (uint32_t)b->views.size();
     b->jobs.assign(n, cfk::ViewJob{});
@@ -251,8 +280,15 @@ namespace cfrt {
 int batch_cull(CfBatch* b, cudaStream_t st)
 {
     DeviceGuard g(b->device);
-    if (!b->use_graph || st == nullptr) return enqueue_batch(b, st);
+    if (!b->use_graph || st == nullptr) {
+        const int s = enqueue_batch(b, st);
+        return s ? s : mark_used(b, st);
+    }
     if (!b->exec || b->graph_stream != st) {
+        if (b->exec) {  // the graph may still run on its former stream
+            const int w = wait_idle(b);
+            if (w) return w;
+        }
         drop_graph(b);
         cudaGraph_t graph = nullptr;
         cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
@@ -273,7 +309,7 @@ int batch_cull(CfBatch* b, cudaStream_t st)
         b->graph_stream = st;
     }
     const cudaError_t e = cudaGraphLaunch(b->exec, st);
-    return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "cudaGraphLaunch");
+    return e == cudaSuccess ? mark_used(b, st) : cuda_fail(e, "cudaGraphLaunch");
 }
 
 }  // namespace cfrt
@@ -291,7 +327,9 @@ int cf_batch_create(CfContext* ctx, CfBatch** out)
     DeviceGuard g(b->device);
     cudaError_t e = cudaMalloc(&b->d_queues, cfk::kMaxBatchQueues * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(b->d_queues, 0, cfk::kMaxBatchQueues * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->last_use, cudaEventDisableTiming);
     if (e != cudaSuccess) {
+        cudaFree(b->d_queues);
         delete b;
         return cuda_fail(e, "batch queues");
     }
@@ -303,7 +341,9 @@ int cf_batch_destroy(CfBatch* b)
 {
     if (!b) return CF_SUCCESS;
     DeviceGuard g(b->device);
+    wait_idle(b);
     drop_graph(b);
+    if (b->last_use) cudaEventDestroy(b->last_use);
     cudaFree(b->d_jobs);
     cudaFree(b->d_prefix);
     cudaFree(b->d_items);
@@ -327,6 +367,8 @@ int cf_batch_update_view_matrices(CfBatch* b, const CfClusterForwardUBO* ubos, u
     if (!b || (n && !ubos)) return fail(CF_ERROR_INVALID_ARGUMENT, "null argument");
     if (n != b->views.size()) return fail(CF_ERROR_INVALID_ARGUMENT, "%u UBOs for %zu views", n, b->views.size());
     DeviceGuard g(b->device);
+    const int w = wait_idle(b);  // a pass queued on another stream may still read the table
+    if (w) return w;
     for (uint32_t i = 0; i < n; ++i) {
         for (int q = 0; q < 16; ++q) b->jobs[i].view[q] = ubos[i].cameraView[q];
         b->views[i].ubo = ubos[i];
@@ -344,7 +386,7 @@ int cf_batch_generate_aabbs(CfBatch* b, void* stream)
     DeviceGuard g(b->device);
     const cudaError_t e = cfk::launch_batch_aabb(b->d_aabb_jobs, b->d_aabb_prefix, (uint32_t)b->views.size(),
                                                  b->aabb_blocks, (cudaStream_t)stream);
-    return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "AABB generator launch");
+    return e == cudaSuccess ? mark_used(b, (cudaStream_t)stream) : cuda_fail(e, "AABB generator launch");
 }
 
 int cf_batch_cull(CfBatch* b, void* stream)
@@ -356,6 +398,8 @@ int cf_batch_cull(CfBatch* b, void* stream)
 int cf_batch_set_graph(CfBatch* b, int enable)
 {
     if (!b) return fail(CF_ERROR_INVALID_ARGUMENT, "null batch");
+    const int w = wait_idle(b);
+    if (w) return w;
     b->use_graph = enable != 0;
     drop_graph(b);
     return CF_SUCCESS;

@@ -572,6 +572,7 @@ int cf_pipeline_light_culling_enable_work_counters(CfPipelineLightCulling* p, in
     if (!p) return fail(CF_ERROR_INVALID_ARGUMENT, "null pipeline");
     DeviceGuard g(p->ctx->device);
     if (!enable) {
+        if (p->d_work) cudaDeviceSynchronize();  // a queued cull may still count into it
         cudaFree(p->d_work);
         p->d_work = nullptr;
         return CF_SUCCESS;

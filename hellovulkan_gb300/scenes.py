@@ -192,3 +192,16 @@ def stress_ubo(view_index: int, epoch: int, camera) -> CfClusterForwardUBO:
     u = CfClusterForwardUBO.from_buffer_copy(_STRESS_PROJ[key])
     u.cameraView[:] = np.asarray(camera, np.float32).T.reshape(-1).tolist()
     return u
+
+
+def depth_log_uniform(rng: np.random.Generator, width: int, height: int, near: float, far: float,
+                      far_plane_fraction: float = 0.0) -> np.ndarray:
+    """A synthetic (height, width) ZO depth buffer: linear depth log-uniform in
+    [near, far), turned into window depth by inverting Scene.frag's
+    LinearDepth; a fraction of the pixels sits on the far plane (depth 1)."""
+    lin = np.exp(rng.uniform(math.log(near), math.log(far), size=(height, width)))
+    z = (near * far / lin - far) / (near - far)
+    z = np.clip(z, 0.0, np.nextafter(np.float32(1.0), np.float32(0.0))).astype(np.float32)
+    if far_plane_fraction > 0:
+        z[rng.uniform(size=z.shape) < far_plane_fraction] = 1.0
+    return z

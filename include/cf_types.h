@@ -75,6 +75,25 @@ typedef struct CfLightOrbit {
     float center[4];                /* x, y, z and the position's w        */
 } CfLightOrbit;
 
+/* What Scene.frag's cluster lookup (Shaders/ClusteredForward/Scene.frag:54-78)
+ * finds for one fragment, and how its light list serves it (cf_lookup_clusters). */
+typedef struct CfFragmentSample {
+    uint32_t cluster;   /* clusterIdx; 0xFFFFFFFF when the lookup leaves the grid     */
+    uint32_t offset;    /* lightCells[clusterIdx].offset                              */
+    uint32_t count;     /* lightCells[clusterIdx].count                               */
+    uint32_t covering;  /* lights of the list whose sphere contains the fragment      */
+    uint32_t missing;   /* (all-lights check) lights NOT in the list that contain it  */
+    uint32_t flags;     /* CF_FRAGMENT_* bits                                         */
+    float view_z;       /* the fragment's view-space z, from its depth                */
+    float linear_depth; /* LinearDepth(gl_FragCoord.z, near, far)                     */
+} CfFragmentSample;
+
+#define CF_FRAGMENT_OUTSIDE_GRID 1u  /* zIndex (or x, y) beyond the grid: no cluster */
+#define CF_FRAGMENT_OUTSIDE_AABB 2u  /* the fragment lies outside its cluster's box   */
+#define CF_FRAGMENT_CAPPED 4u        /* the cluster's list holds the cap of lights     */
+#define CF_FRAGMENT_BAD_CELL 8u      /* the cell points outside the index list, or an
+                                        index is not a light: nothing read through it */
+
 /* Per-view parameters, std140: invProj @0, view @64, screenSize @128,
  * sliceScaling @136, sliceBias @140, near @144, far @148, X/Y/Z @152/156/160.
  * 164 bytes are used; the C++ mirror in the reference is 176 bytes. */
@@ -106,6 +125,7 @@ static_assert(sizeof(CfLightCell) == 8, "LightCell is two uint");
 static_assert(offsetof(CfLightCell, count) == 4, "LightCell.count @4");
 static_assert(sizeof(CfClusterForwardUBO) == 176, "ClusterForwardUBO C++ sizeof");
 static_assert(sizeof(CfLightOrbit) == 32 && offsetof(CfLightOrbit, center) == 16, "LightOrbit is two float4");
+static_assert(sizeof(CfFragmentSample) == 32, "FragmentSample is 32 bytes");
 static_assert(offsetof(CfClusterForwardUBO, cameraView) == 64, "view @64");
 static_assert(offsetof(CfClusterForwardUBO, screenSize) == 128, "screenSize @128");
 static_assert(offsetof(CfClusterForwardUBO, sliceScaling) == 136, "sliceScaling @136");

@@ -228,7 +228,10 @@ typedef struct CfBatchInfo {
 CFCULL_API int cf_batch_create(CfContext* ctx, CfBatch** out);
 CFCULL_API int cf_batch_destroy(CfBatch* batch);
 /* Replaces the batch's views (copied); allocates its workspace and builds its
- * work-item tables.  Synchronous. */
+ * work-item tables.  Synchronous: it first waits for every pass and AABB
+ * generation the batch enqueued (outside a stream capture) to finish, since
+ * those read the tables it rewrites.  cf_batch_set_tuning,
+ * cf_batch_update_view_matrices and cf_batch_set_graph wait the same way. */
 CFCULL_API int cf_batch_set_views(CfBatch* batch, const CfBatchView* views, uint32_t count);
 /* Updates the view matrices (cameraView of each UBO; the projection part must
  * not change) for the next cf_batch_cull.  Synchronises `stream`. */
@@ -374,6 +377,26 @@ CFCULL_API int cf_generate_aabbs(const CfClusterForwardUBO* ubo, CfAABB* d_aabbs
  * for every light at once. */
 CFCULL_API int cf_animate_light_orbits(CfLightData* d_lights, CfLightOrbit* d_orbits, uint64_t count, uint32_t frames,
                                        void* stream);
+/* Scene.frag's cluster lookup (Shaders/ClusteredForward/Scene.frag:54-78)
+ * for every pixel of a depth buffer, as a check that the (offset, count)
+ * cells drop into the reference's fragment pass: d_depth is width x height
+ * window-space depths (0..1, ZO), row-major from the top row, width and
+ * height equal to ubo->screenSize; fragment (x, y) is at the pixel centre.
+ * LinearDepth, log2 and the tile division follow the shader with log2
+ * pinned (cf_log2_pinned).  For each pixel d_out receives the cluster, its
+ * cell, the number of its listed lights whose sphere contains the fragment's
+ * view-space position, and flags; with check_all_lights != 0 also the number
+ * of lights outside the list that contain it (every light is tested), which
+ * is 0 unless the fragment lies outside its cluster's AABB or the list is
+ * capped.  d_aabbs (optional) enables CF_FRAGMENT_OUTSIDE_AABB.  Light lists
+ * must be in ascending light order, as this library writes them; index_count
+ * bounds the index list (a cell reaching beyond it, or an index >= light_count,
+ * is flagged CF_FRAGMENT_BAD_CELL and nothing is read through it). */
+CFCULL_API int cf_lookup_clusters(const CfClusterForwardUBO* ubo, const float* d_depth, uint32_t width,
+                                  uint32_t height, const CfLightCell* d_cells, const uint32_t* d_indices,
+                                  uint64_t index_count, const CfLightData* d_lights, uint32_t light_count,
+                                  uint32_t max_lights_per_cluster, const CfAABB* d_aabbs, int check_all_lights,
+                                  CfFragmentSample* d_out, void* stream);
 /* LightCulling.comp: d_cells[C] and d_indices (capacity >= C * cap) from
  * d_aabbs[C] and d_lights[light_count]; d_total (optional, device) receives
  * the number of indices.  d_workspace: >= cf_cull_workspace_size bytes,

@@ -37,6 +37,8 @@ class Oracle:
         L.cfo_pow.argtypes = [C.c_float, C.c_float]
         L.cfo_log2.argtypes = [C.c_float]
         L.cfo_exp2.argtypes = [C.c_float]
+        L.cfo_lookup_clusters.argtypes = [_P, _P, C.c_uint32, C.c_uint32, _P, _P, C.c_uint64, _P, C.c_uint32,
+                                          C.c_uint32, _P, C.c_int, _P, C.c_int]
         L.cfo_fp_contract_probe.argtypes = []
         L.cfo_max_threads.argtypes = []
         self.lib = L
@@ -63,6 +65,26 @@ class Oracle:
                                C.byref(total), C.byref(executed), threads)
         assert st == 0, st
         return cells, idx[: total.value].copy(), int(executed.value)
+
+    def lookup_clusters(self, ubo, depth: np.ndarray, cells: np.ndarray, indices: np.ndarray, lights: np.ndarray,
+                        cap: int = 150, aabbs: np.ndarray | None = None, check_all: bool = True, threads: int = 0):
+        """Scene.frag's cluster lookup per pixel (cfo_lookup_clusters); a
+        structured array of shape depth.shape with CfFragmentSample fields."""
+        from hellovulkan_gb300._lib import FRAGMENT_DTYPE
+        depth = np.ascontiguousarray(depth, np.float32)
+        h, w = depth.shape
+        cells = np.ascontiguousarray(cells, np.uint32)
+        indices = np.ascontiguousarray(indices, np.uint32)
+        lights = np.ascontiguousarray(lights, np.float32).reshape(-1, 12)
+        out = np.zeros(depth.shape, FRAGMENT_DTYPE)
+        ab = None if aabbs is None else np.ascontiguousarray(aabbs, np.float32)
+        st = self.lib.cfo_lookup_clusters(_ubo_ptr(ubo), depth.ctypes.data, w, h, cells.ctypes.data,
+                                          indices.ctypes.data if indices.size else None, indices.size,
+                                          lights.ctypes.data if lights.size else None, lights.shape[0], cap,
+                                          None if ab is None else ab.ctypes.data, int(check_all), out.ctypes.data,
+                                          threads)
+        assert st == 0, st
+        return out
 
     def pow(self, x: float, y: float) -> float:
         return self.lib.cfo_pow(x, y)

@@ -10,6 +10,8 @@
  *
  *   cfo_generate_aabbs  HelloVulkan/Shaders/ClusteredForward/AABBGenerator.comp:18-89
  *   cfo_cull            HelloVulkan/Shaders/ClusteredForward/LightCulling.comp:26-87
+ *   cfo_lookup_clusters HelloVulkan/Shaders/ClusteredForward/Scene.frag:54-78 (the consumer's
+ *                       cluster lookup), a check of the culled lists
  *
  * with the three implementation-defined parts of GLSL pinned exactly as in
  * include/cf_pinned_math.h (pow, mat4*vec4 summation order, no FMA).  This
@@ -183,6 +185,90 @@ int cfo_cull(const CfClusterForwardUBO* ubo, const CfAABB* aabbs, const CfLightD
     for (int64_t c = 0; c < C; ++c) {
         if (cells[c].count)
             memcpy(indices + cells[c].offset, stage.data() + size_t(c) * cap, sizeof(uint32_t) * cells[c].count);
+    }
+    return 0;
+}
+
+/*
+ * Scene.frag:54-78's cluster lookup for every pixel of a depth buffer
+ * (row-major from the top row, fragment at the pixel centre), with log2
+ * pinned like the kernel (cf_log2_pinned), the fragment unprojected like
+ * AABBGenerator.comp:18-32's ScreenToView, and the containment test
+ * |fragment - light|^2 < r^2 summed x, y, z.  Same outputs as
+ * cf_lookup_clusters (include/cfcull.h).  Returns 0 or 1 (bad argument).
+ */
+int cfo_lookup_clusters(const CfClusterForwardUBO* ubo, const float* depth, uint32_t width, uint32_t height,
+                        const CfLightCell* cells, const uint32_t* indices, uint64_t index_count,
+                        const CfLightData* lights, uint32_t light_count, uint32_t cap, const CfAABB* aabbs,
+                        int check_all, CfFragmentSample* out, int threads)
+{
+    if (!ubo || !depth || !cells || !out) return 1;
+    const CfClusterForwardUBO& u = *ubo;
+    const uint32_t X = u.sliceCountX, Y = u.sliceCountY, Z = u.sliceCountZ;
+    if (cap == 0) cap = 0xFFFFFFFFu;
+    if (threads <= 0) threads = omp_get_max_threads();
+    const int64_t n = int64_t(width) * height;
+    const float* V = u.cameraView;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 256)
+    for (int64_t pix = 0; pix < n; ++pix) {
+        const float x = float(uint32_t(pix % width)) + 0.5f, y = float(uint32_t(pix / width)) + 0.5f;
+        const float zd = depth[pix];
+        const float near_ = u.cameraNear, far_ = u.cameraFar;
+        const float lin = near_ * far_ / (far_ + zd * (near_ - far_));
+        const float zi = gmax(cf_log2_pinned(lin) * u.sliceScaling + u.sliceBias, 0.0f);
+        const float tile_x = u.screenSize[0] / float(X), tile_y = u.screenSize[1] / float(Y);
+        const float xi = x / tile_x, yi = y / tile_y;
+        const V4 screen = {x / u.screenSize[0], y / u.screenSize[1], zd, 1.0f};
+        const V4 clip = {screen.x * 2.0f - 1.0f, screen.y * 2.0f - 1.0f, screen.z, screen.w};
+        const V4 vv = mat_mul(u.cameraInverseProjection, clip);
+        const float fp[3] = {vv.x / vv.w, vv.y / vv.w, vv.z / vv.w};
+        CfFragmentSample r{};
+        r.view_z = fp[2];
+        r.linear_depth = lin;
+        uint32_t first = 0, count = 0;
+        const bool inside = zi < float(Z) && xi < float(X) && yi < float(Y);
+        if (inside) {
+            const uint32_t c = uint32_t(xi) + uint32_t(yi) * X + uint32_t(zi) * X * Y;
+            r.cluster = c;
+            first = cells[c].offset;
+            count = cells[c].count;
+            if (uint64_t(first) + count > index_count) {
+                r.flags |= CF_FRAGMENT_BAD_CELL;
+                count = 0;
+            }
+            if (count >= cap) r.flags |= CF_FRAGMENT_CAPPED;
+            if (aabbs) {
+                const CfAABB& b = aabbs[c];
+                bool out_box = false;
+                for (int a = 0; a < 3; ++a) out_box |= fp[a] < b.minPoint[a] || fp[a] > b.maxPoint[a];
+                if (out_box) r.flags |= CF_FRAGMENT_OUTSIDE_AABB;
+            }
+        } else {
+            r.cluster = 0xFFFFFFFFu;
+            r.flags |= CF_FRAGMENT_OUTSIDE_GRID;
+        }
+        auto covers = [&](uint32_t li) {
+            const CfLightData& L = lights[li];
+            const V4 pv = mat_mul(V, V4{L.position[0], L.position[1], L.position[2], L.position[3]});
+            const float dx = fp[0] - pv.x, dy = fp[1] - pv.y, dz = fp[2] - pv.z;
+            return (dx * dx + dy * dy) + dz * dz < L.radius * L.radius;
+        };
+        std::vector<char> listed(check_all ? light_count : 0, 0);
+        for (uint32_t j = 0; j < count; ++j) {
+            const uint32_t li = indices[first + j];
+            if (li >= light_count) {
+                r.flags |= CF_FRAGMENT_BAD_CELL;
+                continue;
+            }
+            if (check_all) listed[li] = 1;
+            r.covering += covers(li) ? 1u : 0u;
+        }
+        r.offset = first;
+        r.count = (r.flags & CF_FRAGMENT_BAD_CELL) ? 0u : count;
+        if (check_all)
+            for (uint32_t i = 0; i < light_count; ++i)
+                if (!listed[i] && covers(i)) r.missing++;
+        out[pix] = r;
     }
     return 0;
 }

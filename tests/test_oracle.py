@@ -165,3 +165,27 @@ def test_zero_lights_and_cap_of_one(oracle):
     assert idx.size == 0 and not cells.any() and ex == 0
     cells, idx, _ = oracle.cull(v.ubo, a, v.lights, 1)
     assert cells[:, 1].max() == 1 and np.array_equal(cells[:, 0], np.cumsum(cells[:, 1]) - cells[:, 1])
+
+
+def test_oracle_lookup_flags_cells_that_leave_the_index_list(oracle):
+    """A cell pointing past the index list, or at a light that does not exist,
+    is flagged and nothing is read through it (planted in the oracle's inputs)."""
+    from hellovulkan_gb300 import scenes
+    from hellovulkan_gb300._lib import FRAGMENT_BAD_CELL
+    v = scenes.custom_view((4, 3, 8), 40, 30, 0.1, 100.0, lights=scenes.uniform_box_lights(
+        np.random.default_rng(3), 50, [-5, -5, -60], [5, 5, -1]))
+    a = oracle.generate_aabbs(v.ubo)
+    cells, idx, _ = oracle.cull(v.ubo, a, v.lights, 150)
+    depth = scenes.depth_log_uniform(np.random.default_rng(4), 40, 30, 0.1, 100.0)
+    good = oracle.lookup_clusters(v.ubo, depth, cells, idx, v.lights, 150, a)
+    assert not np.any(good["flags"] & FRAGMENT_BAD_CELL) and np.all(good["missing"][good["flags"] == 0] == 0)
+    bad = cells.copy()
+    bad[:, 0] = idx.size + 5  # every offset beyond the list
+    s = oracle.lookup_clusters(v.ubo, depth, bad, idx, v.lights, 150, a)
+    hit = s["count"] == 0
+    assert np.all((s["flags"] & FRAGMENT_BAD_CELL) > 0) and np.all(hit)
+    wrong = idx.copy()
+    wrong[:] = v.light_count + 1  # indices that name no light
+    s = oracle.lookup_clusters(v.ubo, depth, cells, wrong, v.lights, 150, a)
+    listed = good["count"] > 0
+    assert np.all((s["flags"][listed] & FRAGMENT_BAD_CELL) > 0) and np.all(s["covering"] == 0)

@@ -344,21 +344,24 @@ def measure_batch(ctx, stream, n_views=256, passes=20, seed=3, sample_views=6):
     }
 
 
-def measure_serve(ctx, seconds, rates=(2000.0, 10000.0, 50000.0), saturation_rate=200000.0,
-                  saturation_seconds=2.0, submit_threads=4):
+def measure_serve(ctx, seconds, rates=(2000.0, 10000.0, 50000.0), sweep=(20000.0, 30000.0, 40000.0, 50000.0,
+                                                                        60000.0, 80000.0),
+                  sweep_seconds=3.0, submit_threads=4):
     """The served stream: Poisson arrivals at each rate for `seconds`, requests
     drawn like the batched mix (4 projections, random cameras, 128 base light
     sets of 256..65536 blob lights), light sets re-referenced with p = 0.7 and
     jittered on the device by N(0, 0.1) per request, an 8 GiB device budget.
-    Latency runs from the scheduled arrival to the completion callback.  A last
-    run offers far more than the server can take, to measure its capacity."""
+    Latency runs from the scheduled arrival to the completion callback.  A
+    sweep of shorter runs then finds the highest offered rate the server
+    sustains with p99 <= 2 ms (stopping at the first rate that misses)."""
     from hellovulkan_gb300.server import Server, run_load
     keep = ("offered_rate", "achieved_rate", "scheduled", "completed", "failed", "latency_p50_ms", "latency_p90_ms",
-            "latency_p99_ms", "latency_p999_ms", "queue_p50_ms", "queue_p99_ms", "exec_p50_ms", "exec_p99_ms",
-            "submit_lag_p99_ms", "register_call_p50_us", "jitter_call_p50_us", "submit_call_p50_us", "tests_per_s",
-            "new_sets", "reused_sets")
-    runs = []
-    for rate, dur, thr in [(r, seconds, submit_threads) for r in rates] + [(saturation_rate, saturation_seconds, 8)]:
+            "latency_p99_ms", "latency_p999_ms", "latency_max_ms", "queue_p50_ms", "queue_p99_ms", "exec_p50_ms",
+            "exec_p99_ms", "submit_lag_p99_ms", "register_call_p50_us", "jitter_call_p50_us", "submit_call_p50_us",
+            "register_call_max_us", "jitter_call_max_us", "submit_call_max_us", "worst_lag_arrival_s",
+            "tests_per_s", "new_sets", "reused_sets")
+
+    def one(rate, dur, thr):
         srv = Server(ctx, budget_bytes=8 << 30, max_batch_views=64, streams=4)
         rep = run_load(srv, rate=rate, duration=dur, submit_threads=thr)
         st = srv.stats()
@@ -368,12 +371,89 @@ def measure_serve(ctx, seconds, rates=(2000.0, 10000.0, 50000.0), saturation_rat
         r.update({"views_per_s": rep["achieved_rate"], "batches": st["batches"],
                   "mean_views_per_batch": st["views_launched"] / max(1, st["batches"]),
                   "max_batch_views": st["max_batch_views"], "arena_peak_bytes": st["arena_peak_bytes"],
-                  "evictions": st["evictions"], "p99_within_2ms": rep["latency_p99_ms"] <= 2.0})
-        runs.append(r)
+                  "evictions": st["evictions"],
+                  "sustained": rep["latency_p99_ms"] <= 2.0 and rep["failed"] == 0 and
+                  rep["achieved_rate"] >= 0.98 * rep["offered_rate"]})
+        return r
+
+    runs = [one(r, seconds, submit_threads) for r in rates]
+    swept, best = [], 0.0
+    for r in sweep:
+        x = one(r, sweep_seconds, 8)
+        swept.append({k: x[k] for k in ("rate", "achieved_rate", "latency_p50_ms", "latency_p99_ms",
+                                         "mean_views_per_batch", "sustained")})
+        if not x["sustained"]:
+            break
+        best = x["achieved_rate"]
     return {"workload": "Poisson arrivals, 4 projections {8x8x16,16x9x24,24x14x32,32x18x48}, 128 base sets of "
                         "256..65536 blob lights, p_reuse 0.7 with device jitter sigma 0.1, 8 GiB budget, "
                         "64 views per batch, 4 streams",
-            "runs": runs[:-1], "saturation": runs[-1], "capacity_views_per_s": runs[-1]["achieved_rate"]}
+            "runs": runs, "sweep": swept, "sweep_seconds": sweep_seconds,
+            "max_sustained_views_per_s": best,
+            "note": "sustained = p99 <= 2 ms, no failures, achieved >= 98% of offered"}
+
+
+def measure_lookup(ctx, stream, reps=20):
+    """Scene.frag's cluster lookup (cf_lookup_clusters) over a 1920x1080 depth
+    buffer of log-uniform linear depths, on the 1920x1080 16x9x24 view with 1024
+    lights culled by the pipeline: the lookup alone (timed), then once with
+    every light tested (the drop-in check: a light containing a fragment but
+    missing from its list only where the fragment leaves its cluster's box)."""
+    import torch
+
+    from hellovulkan_gb300._lib import FRAGMENT_CAPPED, FRAGMENT_OUTSIDE_AABB
+    from hellovulkan_gb300.consumer import lookup_clusters, samples_to_numpy
+    from hellovulkan_gb300.pipelines import (PipelineAABBGenerator, PipelineLightCulling, ResourcesClusterForward,
+                                             ResourcesLight)
+    from hellovulkan_gb300 import scenes
+    v = scenes.plain_small(1)
+    rl = ResourcesLight(ctx)
+    rl.add_lights(v.lights)
+    rc = ResourcesClusterForward(ctx)
+    rc.create_buffers(*v.grid, v.cap)
+    gen = PipelineAABBGenerator(ctx, rc)
+    gen.set_cluster_forward_ubo(v.ubo)
+    gen.fill_command_buffer(stream)
+    cu = PipelineLightCulling(ctx, rl, rc)
+    cu.set_cluster_forward_ubo(v.ubo)
+    cu.fill_command_buffer(stream)
+    b = rc.buffers()
+    stream.synchronize()
+    _, idx = rc.read_outputs(stream)
+    w, h = 1920, 1080
+    depth = torch.from_numpy(scenes.depth_log_uniform(np.random.default_rng(7), w, h, 0.1, 1000.0)).cuda()
+    def run(check_all):
+        return lookup_clusters(v.ubo, depth, b.light_cells, b.light_indices, rl.device_buffer, idx.size,
+                               v.light_count, v.cap, b.aabbs, check_all, stream)
+
+    for _ in range(3):
+        run(False)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for a, c in ev:
+        a.record(stream)
+        run(False)
+        c.record(stream)
+    torch.cuda.synchronize()
+    ms = float(np.median([a.elapsed_time(c) for a, c in ev]))
+    a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    out = run(True)
+    c.record(stream)
+    torch.cuda.synchronize()
+    check_ms = a.elapsed_time(c)
+    s = samples_to_numpy(out, h, w)
+    f = s["flags"]
+    explained = (f & (FRAGMENT_OUTSIDE_AABB | FRAGMENT_CAPPED)) > 0
+    for o in (cu, gen, rc, rl):
+        o.close()
+    moved = w * h * (4 + 32)  # depth read + sample written; cells, indices and lights come from L2
+    return {"workload": "1920x1080 depth buffer, 16x9x24 grid, 1024 lights (plain_small)",
+            "ms": ms, "pixels_per_s": w * h / (ms * 1e-3), "gbs_depth_and_samples": moved / (ms * 1e-3) / 1e9,
+            "check_all_lights_ms": check_ms, "mean_listed_lights": float(s["count"].mean()),
+            "mean_covering_lights": float(s["covering"].mean()),
+            "pixels_outside_their_box": int((f & FRAGMENT_OUTSIDE_AABB > 0).sum()),
+            "pixels_missing_a_light": int((s["missing"] > 0).sum()),
+            "unexplained_misses": int(((s["missing"] > 0) & ~explained).sum())}
 
 
 def measure_stress(ctx, stream, n_views, n_lights, frames, seed=5):
@@ -518,6 +598,9 @@ def run_ours(args):
     batched = None
     if not args.no_batch and rank == 0:
         batched = measure_batch(ctx, stream)
+    lookup = None
+    if rank == 0:
+        lookup = measure_lookup(ctx, stream)
     stress = None
     if not args.no_stress and rank == 0:
         stress = measure_stress(ctx, stream, args.stress_views, args.stress_lights, args.stress_frames)
@@ -525,8 +608,9 @@ def run_ours(args):
     if not args.no_serve and rank == 0:
         served = measure_serve(ctx, args.serve_seconds)
         if batched:
-            served["speedup_vs_plain_per_view"] = served["capacity_views_per_s"] / batched["plain_per_view_views_per_s"]
-            served["speedup_vs_per_view_launch"] = (served["capacity_views_per_s"] /
+            served["speedup_vs_plain_per_view"] = (served["max_sustained_views_per_s"] /
+                                                   batched["plain_per_view_views_per_s"])
+            served["speedup_vs_per_view_launch"] = (served["max_sustained_views_per_s"] /
                                                     batched["per_view_launch_views_per_s"])
 
     tests_per_view = view.clusters * view.light_count
@@ -619,6 +703,7 @@ def run_ours(args):
         "batched": batched,
         "served": served,
         "stress": stress,
+        "cluster_lookup": lookup,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:

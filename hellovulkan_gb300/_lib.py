@@ -137,12 +137,14 @@ class CfServeReport(C.Structure):
                                   "latency_p99_ms", "latency_p999_ms", "latency_max_ms", "queue_p50_ms",
                                   "queue_p99_ms", "submit_lag_p99_ms", "exec_p50_ms", "exec_p99_ms",
                                   "register_call_p50_us", "register_call_p99_us", "jitter_call_p50_us",
-                                  "jitter_call_p99_us", "submit_call_p50_us", "submit_call_p99_us")]
+                                  "jitter_call_p99_us", "submit_call_p50_us", "submit_call_p99_us",
+                                  "register_call_max_us", "jitter_call_max_us", "submit_call_max_us",
+                                  "worst_lag_arrival_s")]
 
 
 assert C.sizeof(CfServerConfig) == 24 and C.sizeof(CfServerRequest) == 208
 assert C.sizeof(CfServerCompletion) == 72 and C.sizeof(CfServerStats) == 104
-assert C.sizeof(CfServeLoad) == 128 and C.sizeof(CfServeReport) == 208
+assert C.sizeof(CfServeLoad) == 128 and C.sizeof(CfServeReport) == 240
 assert CfServeLoad.projections.offset == 56 and CfServeLoad.eye_lo.offset == 80
 assert C.sizeof(CfBatchView) == 240 and C.sizeof(CfBatchInfo) == 216
 assert C.sizeof(CfLightData) == 48 and C.sizeof(CfAABB) == 32 and C.sizeof(CfLightCell) == 8

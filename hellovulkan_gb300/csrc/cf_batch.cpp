@@ -189,8 +189,8 @@ int rebuild(CfBatch* b)
         aabb_prefix[i] = ab;
         ab += (C + 255) / 256;
         xb += cfk::granules(j.v.lpad);
-        bb += Z;
-        cb += cfk::copy_blocks(C);
+        bb += cfk::bin_blocks(Z);
+        cb += cfk::copy_blocks(groups);
     }
     b->xform_blocks = xb;
     b->bin_blocks = bb;
@@ -259,7 +259,6 @@ int enqueue_batch(CfBatch* b, cudaStream_t st)
     if (n == 0) return CF_SUCCESS;
     const uint32_t* px = b->d_prefix;
     const uint32_t* pb = b->d_prefix + n;
-    const uint32_t* pc = b->d_prefix + 2 * (size_t)n;
     cudaError_t e = cfk::launch_batch_xform(b->d_jobs, px, n, b->xform_blocks, b->d_queues,
                                             (uint32_t)b->buckets.size(), st);
     if (e == cudaSuccess) e = cfk::launch_batch_bin(b->d_jobs, pb, n, b->bin_blocks, st);
@@ -269,7 +268,7 @@ int enqueue_batch(CfBatch* b, cudaStream_t st)
         e = cfk::launch_batch_cull(bc, bk.cfg, bk.ctas, b->dev_error, st);
     }
     if (e == cudaSuccess) e = cfk::launch_batch_scan(b->d_jobs, n, st);
-    if (e == cudaSuccess) e = cfk::launch_batch_copy(b->d_jobs, pc, n, b->copy_blocks_total, st);
+    if (e == cudaSuccess) e = cfk::launch_batch_copy(b->d_jobs, b->d_prefix + 2 * (size_t)n, n, b->copy_blocks_total, st);
     return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "batch launch");
 }
 

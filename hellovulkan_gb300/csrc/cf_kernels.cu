@@ -90,6 +90,18 @@ __device__ __noinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
     return false;
 }
 
+// As mbar_wait_bounded, but also gives up (returning false) once *abort is set.
+__device__ __noinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity, const volatile uint32_t* abort)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_timer_ns();
+    for (uint32_t it = 0; it < kWaitLimitIters; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (*abort || global_timer_ns() - t0 > kWaitLimitNs) break;
+    }
+    return false;
+}
+
 __device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar)
 {
     asm volatile(
@@ -717,33 +729,339 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
     cull_group<K, WARPS, TILE, STAGES, kBinned>(v, blockIdx.x, sm, 0, &s_used, &s_abort, dev_error);
 }
 
-// Many views in one persistent launch: each CTA takes (view, group) items from
-// `items` in queue order (an atomic counter the light-transform launch resets)
-// until none are left.  Items are ordered by decreasing expected work, so the
-// longest ones start first.
-template <int K, int WARPS, int TILE, int STAGES, bool kBinned>
-__global__ void __launch_bounds__((WARPS + 1) * 32)
-    cull_batch_kernel(const ViewJob* __restrict__ jobs, const uint2* __restrict__ items, uint32_t n_items,
-                      uint32_t* __restrict__ queue, uint32_t* __restrict__ dev_error)
+// Many views in one persistent launch (binned culling).  Each CTA takes
+// (view, group) items from `items` in queue order (an atomic counter the
+// light-transform launch resets) until none are left; items are ordered by
+// decreasing expected work.  The producer warp runs ahead of the consumers:
+// while they cull item n it already fetches item n + 1, writes its descriptor
+// into a ring of kItemSlots shared-memory slots, loads the group's AABBs into
+// the slot and starts streaming the item's candidate tiles through the stage
+// ring.  So the latency of the item's global reads and first copies is hidden
+// behind the previous item.  Stage tiles are numbered across items (the
+// descriptor carries the item's first tile number), which fixes each tile's
+// stage and mbarrier phases.
+constexpr uint32_t kItemSlots = 2;
+
+struct ItemDesc {
+    uint32_t* staging;
+    uint32_t* counts;
+    uint32_t* group_sums;
+    unsigned long long* work;
+    uint32_t first, cl_end, nsrc, ntiles;
+    uint32_t seq, group, cap, flags;  // flags: kItemTerminate | kItemExact
+};
+static_assert(sizeof(ItemDesc) % 16 == 0, "descriptor slots stay 16-byte aligned");
+constexpr uint32_t kItemTerminate = 1u, kItemExact = 2u;
+
+// Dynamic shared memory of cull_pipe_kernel: stage tiles and their light
+// indices, kItemSlots groups of AABBs, the survivor buffer, kItemSlots
+// descriptors, the mbarriers, then small words.
+template <int K, int WARPS, int TILE, int STAGES>
+struct PipeSmem {
+    static constexpr uint32_t kGroup = (uint32_t)(K * WARPS);
+    static constexpr size_t tiles = 0;
+    static constexpr size_t idx = tiles + (size_t)STAGES * TILE * sizeof(float4);
+    static constexpr size_t boxes = idx + (size_t)STAGES * TILE * sizeof(uint32_t);
+    static constexpr size_t surv_l = boxes + (size_t)kItemSlots * kGroup * sizeof(CfAABB);
+    static constexpr size_t surv_i = surv_l + (size_t)TILE * sizeof(float4);
+    static constexpr size_t desc = surv_i + (size_t)TILE * sizeof(uint32_t);
+    static constexpr size_t bars = desc + kItemSlots * sizeof(ItemDesc);
+    static constexpr size_t small = bars + (2 * STAGES + 2 * kItemSlots) * sizeof(uint64_t);
+    // stop[STAGES], done[kItemSlots], chunk counts[TILE / 32], boxes[WARPS * 8], warp sums[WARPS], the
+    // consumers' abort flag, the producer's abort flag
+    static constexpr size_t bytes = small + (STAGES + kItemSlots + TILE / 32 + WARPS * 8 + WARPS + 2) * 4;
+    static_assert(boxes % 16 == 0 && desc % 16 == 0 && bars % 8 == 0, "shared-memory alignment");
+};
+
+template <int K, int WARPS, int TILE, int STAGES>
+__global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 4 : 2)
+    cull_pipe_kernel(const ViewJob* __restrict__ jobs, const uint2* __restrict__ items, uint32_t n_items,
+                     uint32_t* __restrict__ queue, uint32_t* __restrict__ dev_error, const ViewCull single)
 {
+    // jobs == nullptr: one view (`single`), item i is its group i
+    static_assert(TILE % 32 == 0 && TILE / 32 <= 32, "tiles hold whole warps of lights, at most 32 chunks");
+    using Lay = PipeSmem<K, WARPS, TILE, STAGES>;
+    constexpr uint32_t kGroup = Lay::kGroup;
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ uint32_t s_item, s_used, s_abort;
-    CullSmem<K, WARPS, TILE, STAGES, kBinned> sm(smem);
-    sm.init();
-    if (threadIdx.x == 0) s_abort = 0;
-    uint32_t seq = 0;
-    for (;;) {
-        if (threadIdx.x == 0) {  // s_used is written by the producer before the barrier below
-            s_item = atomicAdd(queue, 1u);
-            *sm.done_warps = 0;
+    float4* const tiles = reinterpret_cast<float4*>(smem + Lay::tiles);
+    uint32_t* const idx_tiles = reinterpret_cast<uint32_t*>(smem + Lay::idx);
+    float4* const boxes = reinterpret_cast<float4*>(smem + Lay::boxes);
+    float4* const surv_l = reinterpret_cast<float4*>(smem + Lay::surv_l);
+    uint32_t* const surv_i = reinterpret_cast<uint32_t*>(smem + Lay::surv_i);
+    ItemDesc* const desc = reinterpret_cast<ItemDesc*>(smem + Lay::desc);
+    uint64_t* const full = reinterpret_cast<uint64_t*>(smem + Lay::bars);
+    uint64_t* const empty = full + STAGES;
+    uint64_t* const ifull = empty + STAGES;
+    uint64_t* const iempty = ifull + kItemSlots;
+    volatile uint32_t* const stop = reinterpret_cast<volatile uint32_t*>(smem + Lay::small);
+    uint32_t* const done = const_cast<uint32_t*>(stop) + STAGES;  // per slot: consumer warps all capped
+    uint32_t* const s_cnt = done + kItemSlots;
+    float* const s_box = reinterpret_cast<float*>(s_cnt + TILE / 32);
+    uint32_t* const s_gsum = reinterpret_cast<uint32_t*>(s_box + WARPS * 8);
+    // s_abort is written only by consumer threads, before a consumer barrier,
+    // so every consumer warp reads the same value after it; the producer
+    // keeps its own flag and the consumers learn of its failure through their
+    // own bounded waits.
+    volatile uint32_t* const s_abort = s_gsum + WARPS;
+    volatile uint32_t* const p_abort = s_gsum + WARPS + 1;
+
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), WARPS);
+            stop[s] = 0;
         }
-        __syncthreads();
-        const uint32_t it = s_item;
-        if (it >= n_items || s_abort) break;
-        const uint2 item = items[it];
-        cull_group<K, WARPS, TILE, STAGES, kBinned>(jobs[item.x].v, item.y, sm, seq, &s_used, &s_abort, dev_error);
-        __syncthreads();
-        seq += s_used;
+        for (uint32_t r = 0; r < kItemSlots; ++r) {
+            mbar_init(smem_u32(&ifull[r]), 1);
+            mbar_init(smem_u32(&iempty[r]), WARPS);
+            done[r] = 0;
+        }
+        *s_abort = 0;
+        *p_abort = 0;
+        mbar_init_fence();
+    }
+    __syncthreads();
+
+    if (warp == WARPS) {
+        // Producer: lane 0 fetches items, fills descriptors, loads AABBs and
+        // streams candidate tiles; it never waits for the consumers to finish
+        // an item, only for a free descriptor slot and free stages.
+        if (lane != 0) return;
+        uint32_t seq = 0;        // tiles issued so far
+        uint32_t filled = 0;     // items whose descriptor and boxes were issued
+        for (uint32_t n = 0;; ++n) {
+            const uint32_t r = n % kItemSlots;
+            if (n >= kItemSlots &&
+                !mbar_wait_or_abort(smem_u32(&iempty[r]), ((n / kItemSlots) & 1u) ^ 1u, s_abort)) {
+                if (!*s_abort) atomicOr(dev_error, kErrEmptyWaitTimeout);
+                *p_abort = 1;
+                break;
+            }
+            ItemDesc& d = desc[r];
+            const uint32_t it = *s_abort ? n_items : atomicAdd(queue, 1u);
+            if (it >= n_items) {
+                d.flags = kItemTerminate;
+                mbar_arrive(smem_u32(&ifull[r]));
+                break;
+            }
+            const uint2 item = jobs ? items[it] : make_uint2(0u, it);
+            const ViewCull& v = jobs ? jobs[item.x].v : single;
+            const uint32_t xy = v.slice_clusters, gps = (xy + kGroup - 1) / kGroup;
+            const uint32_t k = item.y / gps, g = item.y % gps;
+            const uint32_t first = k * xy + g * kGroup, cl_end = (k + 1) * xy;
+            const uint32_t nb = min(kGroup, cl_end - first);
+            const uint32_t nsrc = v.slice_count[k];
+            const uint32_t ntiles = (nsrc + TILE - 1) / TILE;
+            d.staging = v.staging;
+            d.counts = v.counts;
+            d.group_sums = v.group_sums;
+            d.work = v.work;
+            d.first = first;
+            d.cl_end = cl_end;
+            d.nsrc = nsrc;
+            d.ntiles = ntiles;
+            d.seq = seq;
+            d.group = item.y;
+            d.cap = v.cap;
+            d.flags = v.slice_nonfinite[k] ? kItemExact : 0u;
+            done[r] = 0;
+            mbar_arrive_expect_tx(smem_u32(&ifull[r]), nb * (uint32_t)sizeof(CfAABB));
+            bulk_copy_g2s(smem_u32(boxes + (size_t)r * kGroup * 2), v.aabbs + 2 * (size_t)first,
+                          nb * (uint32_t)sizeof(CfAABB), smem_u32(&ifull[r]));
+            filled = n + 1;
+            const float4* src = v.slice_lights + (size_t)k * v.lpad;
+            const uint32_t* src_idx = v.slice_idx + (size_t)k * v.lpad;
+            uint32_t t = 0;
+            bool stalled = false;
+            for (; t < ntiles; ++t) {
+                const uint32_t gt = seq + t, s = gt % STAGES;
+                if (gt >= STAGES &&
+                    !mbar_wait_or_abort(smem_u32(&empty[s]), ((gt / STAGES) & 1u) ^ 1u, s_abort)) {
+                    if (!*s_abort) atomicOr(dev_error, kErrEmptyWaitTimeout);
+                    *p_abort = 1;
+                    stalled = true;
+                    break;
+                }
+                if (*reinterpret_cast<volatile uint32_t*>(&done[r]) >= (uint32_t)WARPS) {
+                    stop[s] = 1;  // every consumer warp is capped: release them without data
+                    mbar_arrive(smem_u32(&full[s]));
+                    ++t;
+                    break;
+                }
+                stop[s] = 0;
+                const uint32_t cnt = min((uint32_t)TILE, nsrc - t * TILE);
+                mbar_arrive_expect_tx(smem_u32(&full[s]), cnt * (uint32_t)(sizeof(float4) + sizeof(uint32_t)));
+                bulk_copy_g2s(smem_u32(tiles + (size_t)s * TILE), src + (size_t)t * TILE,
+                              cnt * (uint32_t)sizeof(float4), smem_u32(&full[s]));
+                bulk_copy_g2s(smem_u32(idx_tiles + (size_t)s * TILE), src_idx + (size_t)t * TILE,
+                              cnt * (uint32_t)sizeof(uint32_t), smem_u32(&full[s]));
+            }
+            seq += t;
+            if (stalled) break;
+        }
+        if (*p_abort || *s_abort) {
+            // Let every copy this CTA issued land before it exits: the last
+            // tile of each stage and the last item's boxes complete last.
+            for (uint32_t q = 0; q < STAGES && q < seq; ++q) {
+                const uint32_t g = seq - 1 - q;
+                mbar_wait_bounded(smem_u32(&full[g % STAGES]), (g / STAGES) & 1u);
+            }
+            if (filled) mbar_wait_bounded(smem_u32(&ifull[(filled - 1) % kItemSlots]), ((filled - 1) / kItemSlots) & 1u);
+        }
+        return;
+    }
+
+    // Consumers.
+    constexpr uint32_t kChunks = TILE / 32;
+    constexpr int kPer = (int)((kChunks + WARPS - 1) / WARPS);
+    const float inf = __uint_as_float(0x7f800000u);
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    for (uint32_t n = 0;; ++n) {
+        const uint32_t r = n % kItemSlots;
+        if (!mbar_wait_bounded(smem_u32(&ifull[r]), (n / kItemSlots) & 1u) && lane == 0) {
+            atomicOr(dev_error, kErrFullWaitTimeout);
+            *s_abort = 1;
+        }
+        consumer_sync<WARPS * 32>();  // every warp leaves together on a timeout
+        if (*s_abort) break;
+        const ItemDesc d = desc[r];
+        if (d.flags & kItemTerminate) break;
+        const uint32_t cl0 = d.first + warp * (uint32_t)K;
+        const float4* gb = boxes + (size_t)r * kGroup * 2 + (size_t)warp * K * 2;
+        WarpClusters<K> w;
+        bool wdone = true, union_nan = false;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            w.umn[a] = inf;
+            w.umx[a] = -inf;
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            w.cnt[k] = 0;
+            if (cl0 + k < d.cl_end) {
+                const float4 lo = gb[2 * k], hi = gb[2 * k + 1];
+                w.mn[k][0] = lo.x; w.mn[k][1] = lo.y; w.mn[k][2] = lo.z;
+                w.mx[k][0] = hi.x; w.mx[k][1] = hi.y; w.mx[k][2] = hi.z;
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    union_nan |= (w.mn[k][q] != w.mn[k][q]) | (w.mx[k][q] != w.mx[k][q]);
+                    w.umn[q] = fminf(w.umn[q], w.mn[k][q]);
+                    w.umx[q] = fmaxf(w.umx[q], w.mx[k][q]);
+                }
+                wdone = false;
+            } else {
+                for (int q = 0; q < 3; ++q) { w.mn[k][q] = inf; w.mx[k][q] = inf; }
+            }
+        }
+        if (union_nan) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                w.umn[a] = -inf;
+                w.umx[a] = inf;
+            }
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                s_box[warp * 8 + a] = w.umn[a];
+                s_box[warp * 8 + 3 + a] = w.umx[a];
+            }
+            if (wdone) atomicAdd(&done[r], 1u);
+        }
+        consumer_sync<WARPS * 32>();
+        float cmn[3] = {inf, inf, inf}, cmx[3] = {-inf, -inf, -inf};
+        for (int q = 0; q < WARPS; ++q) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                cmn[a] = fminf(cmn[a], s_box[q * 8 + a]);
+                cmx[a] = fmaxf(cmx[a], s_box[q * 8 + 3 + a]);
+            }
+        }
+        const bool exact = (d.flags & kItemExact) != 0;
+        uint32_t chunks_filtered = 0, chunks_tested = 0;
+        for (uint32_t t = 0; t < d.ntiles; ++t) {
+            const uint32_t g = d.seq + t, s = g % STAGES;
+            if (!mbar_wait_bounded(smem_u32(&full[s]), (g / STAGES) & 1u) && lane == 0) {
+                atomicOr(dev_error, kErrFullWaitTimeout);
+                *s_abort = 1;
+            }
+            consumer_sync<WARPS * 32>();
+            if (*s_abort) break;
+            if (stop[s]) {
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&empty[s]));
+                break;
+            }
+            const uint32_t cnt = min((uint32_t)TILE, d.nsrc - t * TILE);
+            const float4* tile = tiles + (size_t)s * TILE;
+            const uint32_t* itile = idx_tiles + (size_t)s * TILE;
+            float4 Ls[kPer];
+            uint32_t Is[kPer], Ms[kPer];
+#pragma unroll
+            for (int q = 0; q < kPer; ++q) {
+                const uint32_t ch = warp + q * WARPS;
+                bool pass = false;
+                if (ch < kChunks && ch * 32 < cnt) {
+                    Ls[q] = tile[ch * 32 + lane];
+                    Is[q] = itile[ch * 32 + lane];
+                    pass = hit_fast(Ls[q], cmn, cmx);
+                    ++chunks_filtered;
+                }
+                Ms[q] = __ballot_sync(kFull, pass);
+                if (ch < kChunks && lane == 0) s_cnt[ch] = __popc(Ms[q]);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&empty[s]));  // the stage is no longer read
+            consumer_sync<WARPS * 32>();
+            const uint32_t c = lane < kChunks ? s_cnt[lane] : 0u;
+            const uint32_t incl = warp_inclusive_scan(c, lane);
+            const uint32_t ns = __shfl_sync(kFull, incl, 31);
+#pragma unroll
+            for (int q = 0; q < kPer; ++q) {
+                const uint32_t ch = warp + q * WARPS;
+                const uint32_t excl = __shfl_sync(kFull, incl - c, ch & 31);
+                if (ch < kChunks && ((Ms[q] >> lane) & 1u)) {
+                    const uint32_t p = excl + __popc(Ms[q] & lt_mask);
+                    surv_l[p] = Ls[q];
+                    surv_i[p] = Is[q];
+                }
+            }
+            const uint32_t nsp = (ns + 31) & ~31u;
+            if (warp == 0 && ns + lane < nsp) surv_l[ns + lane] = make_float4(0.f, 0.f, 0.f, -inf);
+            consumer_sync<WARPS * 32>();
+            if (!wdone && ns) {
+                wdone = exact ? scan_tile<K, true, true>(surv_l, surv_i, nsp, 0, lane, w, d.cap, d.staging, cl0,
+                                                         d.cl_end, chunks_filtered, chunks_tested)
+                              : scan_tile<K, false, true>(surv_l, surv_i, nsp, 0, lane, w, d.cap, d.staging, cl0,
+                                                          d.cl_end, chunks_filtered, chunks_tested);
+                if (wdone && lane == 0) atomicAdd(&done[r], 1u);
+            }
+            consumer_sync<WARPS * 32>();  // the survivor buffer is rewritten by the next tile
+        }
+        if (*s_abort) break;
+        if (lane == 0) {
+            uint32_t sum = 0;
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if (cl0 + k < d.cl_end) {
+                    d.counts[cl0 + k] = w.cnt[k];
+                    sum += w.cnt[k];
+                }
+            s_gsum[warp] = sum;
+            if (d.work) {
+                atomicAdd(&d.work[0], 32ull * chunks_filtered);
+                atomicAdd(&d.work[1], 32ull * K * chunks_tested);
+            }
+        }
+        consumer_sync<WARPS * 32>();
+        if (threadIdx.x == 0) {
+            uint32_t sum = 0;
+            for (int q = 0; q < WARPS; ++q) sum += s_gsum[q];
+            d.group_sums[d.group] = sum;
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(&iempty[r]));  // slot r (descriptor, boxes, done count) is free
     }
 }
 
@@ -756,119 +1074,154 @@ __global__ void __launch_bounds__((WARPS + 1) * 32)
 // squares is never smaller than its z term.  NaN bounds make the slab
 // infinite; a NaN coordinate contributes 0 and is kept; slices holding a
 // light with a non-finite coordinate are flagged for the exact test.
-// One 256-thread CTA per slice; each iteration bins 1024 lights (4 chunks of
-// 32 per warp) with ballot/popc and a block prefix over the 8 warps.
+// One CTA of WARPS warps bins SLICES consecutive slices: every light it reads
+// is tested against each of their slabs, so the view-space lights are read
+// once per SLICES slices (a batch bins 4 slices per 512-thread CTA; a single
+// view, which has few slices, one slice per 1024-thread CTA).  Each step bins
+// WARPS x 128 lights (4 chunks of 32 per warp) with ballot/popc and, per
+// slice, a warp scan of the warps' counts.
 // ---------------------------------------------------------------------------
-constexpr int kBinWarps = 32;
 constexpr int kBinChunks = 4;
+constexpr int kBinWarpsSingle = 32, kBinSlicesSingle = 1;
+constexpr int kBinWarpsBatch = 16, kBinSlicesBatch = 4;
 
-__device__ __forceinline__ void bin_slice_body(const ViewCull& v, uint32_t k)
+template <int kBinWarps, int kBinSlicesT>
+__device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
 {
-    __shared__ float s_lo[kBinWarps], s_hi[kBinWarps];
-    __shared__ uint32_t s_cnt[kBinWarps];
-    __shared__ int s_nan, s_nonfinite;
+    constexpr uint32_t kBinSlices = (uint32_t)kBinSlicesT;
+    __shared__ float s_lo[kBinSlices][kBinWarps], s_hi[kBinSlices][kBinWarps];
+    __shared__ uint32_t s_cnt[kBinSlices][kBinWarps];
+    __shared__ uint32_t s_nan, s_nonfinite;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t xy = v.slice_clusters;
+    const uint32_t xy = v.slice_clusters, k0 = blk * kBinSlices;
+    const uint32_t ns = min(kBinSlices, v.slices - k0);
     const float inf = __uint_as_float(0x7f800000u);
-
-    float lo = inf, hi = -inf;
-    bool nan = false;
-    for (uint32_t c = tid; c < xy; c += kBinWarps * 32) {
-        const float a = v.aabbs[2 * ((size_t)k * xy + c)].z;
-        const float b = v.aabbs[2 * ((size_t)k * xy + c) + 1].z;
-        nan |= (a != a) | (b != b);
-        lo = fminf(lo, a);
-        hi = fmaxf(hi, b);
+    if (tid == 0) {
+        s_nan = 0;
+        s_nonfinite = 0;
+        if (k0 == 0 && v.queue) *v.queue = 0u;  // the single-view culling launch's item counter
     }
+    __syncthreads();
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        lo = fminf(lo, __shfl_xor_sync(kFull, lo, o));
-        hi = fmaxf(hi, __shfl_xor_sync(kFull, hi, o));
+    for (uint32_t sl = 0; sl < kBinSlices; ++sl) {
+        float lo = inf, hi = -inf;
+        bool nan = false;
+        if (sl < ns) {
+            const size_t c0 = (size_t)(k0 + sl) * xy;
+            for (uint32_t c = tid; c < xy; c += kBinWarps * 32) {
+                const float a = v.aabbs[2 * (c0 + c)].z;
+                const float b = v.aabbs[2 * (c0 + c) + 1].z;
+                nan |= (a != a) | (b != b);
+                lo = fminf(lo, a);
+                hi = fmaxf(hi, b);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = fminf(lo, __shfl_xor_sync(kFull, lo, o));
+            hi = fmaxf(hi, __shfl_xor_sync(kFull, hi, o));
+        }
+        if (lane == 0) {
+            s_lo[sl][warp] = lo;
+            s_hi[sl][warp] = hi;
+        }
+        if (nan) atomicOr(&s_nan, 1u << sl);
     }
-    if (tid == 0) s_nonfinite = 0;
-    if (lane == 0) {
-        s_lo[warp] = lo;
-        s_hi[warp] = hi;
-    }
-    const int any_nan = __syncthreads_or(nan);
-    lo = s_lo[0];
-    hi = s_hi[0];
-    for (int q = 1; q < kBinWarps; ++q) {
-        lo = fminf(lo, s_lo[q]);
-        hi = fmaxf(hi, s_hi[q]);
-    }
-    if (any_nan) {
-        lo = -inf;
-        hi = inf;
+    __syncthreads();
+    float lo[kBinSlices], hi[kBinSlices];
+#pragma unroll
+    for (uint32_t sl = 0; sl < kBinSlices; ++sl) {
+        lo[sl] = s_lo[sl][0];
+        hi[sl] = s_hi[sl][0];
+        for (int q = 1; q < kBinWarps; ++q) {
+            lo[sl] = fminf(lo[sl], s_lo[sl][q]);
+            hi[sl] = fmaxf(hi[sl], s_hi[sl][q]);
+        }
+        if ((s_nan >> sl) & 1u) {
+            lo[sl] = -inf;
+            hi[sl] = inf;
+        }
     }
 
-    float4* out_l = v.slice_lights + (size_t)k * v.lpad;
-    uint32_t* out_i = v.slice_idx + (size_t)k * v.lpad;
     const uint32_t lt_mask = (1u << lane) - 1u;
-    uint32_t running = 0;
-    bool nonfinite = false;
+    uint32_t running[kBinSlices] = {};
+    uint32_t nonfinite = 0;  // bit sl: this thread binned a non-finite light into slice sl
     constexpr uint32_t kStep = kBinWarps * kBinChunks * 32;
     for (uint32_t base = 0; base < v.lpad; base += kStep) {
         float4 L[kBinChunks];
-        uint32_t m[kBinChunks];
-        uint32_t wcount = 0;
+        bool fin[kBinChunks];
 #pragma unroll
         for (int q = 0; q < kBinChunks; ++q) {
             const uint32_t i = base + warp * (kBinChunks * 32) + q * 32 + lane;
             L[q] = i < v.lpad ? v.vlights[i] : make_float4(0.f, 0.f, 0.f, -inf);
-            const float dz = max3f(__fsub_rn(lo, L[q].z), __fsub_rn(L[q].z, hi), 0.0f);
-            const bool pass = __fmul_rn(dz, dz) < L[q].w;
-            nonfinite |= pass && !(finite_bits(L[q].x) && finite_bits(L[q].y) && finite_bits(L[q].z));
-            m[q] = __ballot_sync(kFull, pass);
-            wcount += __popc(m[q]);
+            fin[q] = finite_bits(L[q].x) && finite_bits(L[q].y) && finite_bits(L[q].z);
         }
-        if (lane == 0) s_cnt[warp] = wcount;
-        __syncthreads();
-        uint32_t pos = running, total = 0;
+        uint32_t m[kBinSlices][kBinChunks];
 #pragma unroll
-        for (int q = 0; q < kBinWarps; ++q) {
-            const uint32_t cq = s_cnt[q];
-            pos += (q < (int)warp) ? cq : 0u;
-            total += cq;
-        }
+        for (uint32_t sl = 0; sl < kBinSlices; ++sl) {
+            uint32_t wcount = 0;
 #pragma unroll
-        for (int q = 0; q < kBinChunks; ++q) {
-            if ((m[q] >> lane) & 1u) {
-                const uint32_t p = pos + __popc(m[q] & lt_mask);
-                out_l[p] = L[q];
-                out_i[p] = base + warp * (kBinChunks * 32) + q * 32 + lane;
+            for (int q = 0; q < kBinChunks; ++q) {
+                const float dz = max3f(__fsub_rn(lo[sl], L[q].z), __fsub_rn(L[q].z, hi[sl]), 0.0f);
+                const bool pass = sl < ns && __fmul_rn(dz, dz) < L[q].w;
+                nonfinite |= (pass && !fin[q]) ? (1u << sl) : 0u;
+                m[sl][q] = __ballot_sync(kFull, pass);
+                wcount += __popc(m[sl][q]);
             }
-            pos += __popc(m[q]);
+            if (lane == 0) s_cnt[sl][warp] = wcount;
         }
-        running += total;
-        __syncthreads();  // s_cnt is rewritten next iteration
+        __syncthreads();
+#pragma unroll
+        for (uint32_t sl = 0; sl < kBinSlices; ++sl) {
+            if (sl >= ns) break;
+            const uint32_t c = lane < kBinWarps ? s_cnt[sl][lane] : 0u;
+            const uint32_t incl = warp_inclusive_scan(c, lane);
+            uint32_t pos = running[sl] + __shfl_sync(kFull, incl - c, warp);
+            float4* out_l = v.slice_lights + (size_t)(k0 + sl) * v.lpad;
+            uint32_t* out_i = v.slice_idx + (size_t)(k0 + sl) * v.lpad;
+#pragma unroll
+            for (int q = 0; q < kBinChunks; ++q) {
+                if ((m[sl][q] >> lane) & 1u) {
+                    const uint32_t p = pos + __popc(m[sl][q] & lt_mask);
+                    out_l[p] = L[q];
+                    out_i[p] = base + warp * (kBinChunks * 32) + q * 32 + lane;
+                }
+                pos += __popc(m[sl][q]);
+            }
+            running[sl] += __shfl_sync(kFull, incl, 31);
+        }
+        __syncthreads();  // s_cnt is rewritten next step
     }
-    if (nonfinite) s_nonfinite = 1;
-    const uint32_t npad = (running + 31) & ~31u;
-    for (uint32_t p = running + tid; p < npad; p += kBinWarps * 32) {
-        out_l[p] = make_float4(0.f, 0.f, 0.f, -inf);
-        out_i[p] = 0;
+    if (nonfinite) atomicOr(&s_nonfinite, nonfinite);
+#pragma unroll
+    for (uint32_t sl = 0; sl < kBinSlices; ++sl) {
+        if (sl >= ns) break;
+        const uint32_t npad = (running[sl] + 31) & ~31u;
+        float4* out_l = v.slice_lights + (size_t)(k0 + sl) * v.lpad;
+        uint32_t* out_i = v.slice_idx + (size_t)(k0 + sl) * v.lpad;
+        for (uint32_t p = running[sl] + tid; p < npad; p += kBinWarps * 32) {
+            out_l[p] = make_float4(0.f, 0.f, 0.f, -inf);
+            out_i[p] = 0;
+        }
+        if (tid == 0) v.slice_count[k0 + sl] = npad;
     }
     __syncthreads();
-    if (tid == 0) {
-        v.slice_count[k] = npad;
-        v.slice_nonfinite[k] = s_nonfinite ? 1u : 0u;
-        if (v.work) atomicAdd(&v.work[0], (unsigned long long)v.lpad);
-    }
+    if (tid < ns) v.slice_nonfinite[k0 + tid] = (s_nonfinite >> tid) & 1u;
+    if (tid == 0 && v.work) atomicAdd(&v.work[0], (unsigned long long)v.lpad * ns);
 }
 
-__global__ void __launch_bounds__(kBinWarps * 32) bin_slices_kernel(const ViewCull v)
+__global__ void __launch_bounds__(kBinWarpsSingle * 32) bin_slices_kernel(const ViewCull v)
 {
-    bin_slice_body(v, blockIdx.x);
+    bin_slices_body<kBinWarpsSingle, kBinSlicesSingle>(v, blockIdx.x);
 }
 
-// Batched binning: block b is slice b - prefix[v] of view v.
-__global__ void __launch_bounds__(kBinWarps * 32) batch_bin_kernel(const ViewJob* __restrict__ jobs,
-                                                                   const uint32_t* __restrict__ prefix,
-                                                                   uint32_t n_views)
+// Batched binning: block b is slice block b - prefix[v] of view v.
+__global__ void __launch_bounds__(kBinWarpsBatch * 32, 2) batch_bin_kernel(const ViewJob* __restrict__ jobs,
+                                                                        const uint32_t* __restrict__ prefix,
+                                                                        uint32_t n_views)
 {
     const uint32_t vi = find_view(prefix, n_views, blockIdx.x);
-    bin_slice_body(jobs[vi].v, blockIdx.x - __ldg(&prefix[vi]));
+    bin_slices_body<kBinWarpsBatch, kBinSlicesBatch>(jobs[vi].v, blockIdx.x - __ldg(&prefix[vi]));
 }
 
 // ---------------------------------------------------------------------------
@@ -928,6 +1281,7 @@ __device__ __forceinline__ void scan_body(const ViewCull& v)
 // and a warp sum), then its staging slice is copied (at most cap / 32
 // coalesced iterations).  Every warp's loads are independent of the others'.
 constexpr uint32_t kCopyWarps = 8;
+constexpr uint32_t kCopyIlp = 8;
 __global__ void __launch_bounds__(kScanThreads) scan_kernel(const ViewCull v)
 {
     scan_body(v);
@@ -939,27 +1293,46 @@ __global__ void __launch_bounds__(kScanThreads) batch_scan_kernel(const ViewJob*
     scan_body(jobs[blockIdx.x].v);
 }
 
+// One warp per cluster group: the group's cells from its counts (a warp
+// scan on top of the group's offset), then its hits moved from the staging
+// rows to the packed list, 32 at a time across the group's clusters (each
+// lane finds its cluster by a binary search over the warp's exclusive sums).
 __device__ __forceinline__ void copy_body(const ViewCull& v, uint32_t blk)
 {
-    const uint32_t c = blk * kCopyWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (c >= v.clusters) return;
-    uint32_t b, first;
-    if (v.binned) {
-        const uint32_t gps = (v.slice_clusters + v.group_width - 1) / v.group_width;
-        const uint32_t k = c / v.slice_clusters, gi = (c % v.slice_clusters) / v.group_width;
-        b = k * gps + gi;
-        first = k * v.slice_clusters + gi * v.group_width;
-    } else {
-        b = c / v.group_width;
-        first = b * v.group_width;
+    const uint32_t b = blk * kCopyWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (b >= v.groups) return;
+    uint32_t first, end;
+    group_range(v, b, &first, &end);
+    const uint32_t c = first + lane;
+    const uint32_t cnt = c < end ? v.counts[c] : 0u;
+    const uint32_t incl = warp_inclusive_scan(cnt, lane);
+    const uint32_t excl = incl - cnt;
+    const uint32_t base = v.group_offsets[b];
+    if (c < end) v.cells[c] = CfLightCell{base + excl, cnt};
+    const uint32_t total = __shfl_sync(kFull, incl, 31);
+    // kCopyIlp independent loads in flight per lane: a group of capped
+    // clusters holds thousands of hits and its warp sets the launch's length
+    for (uint32_t i0 = 0; i0 < total; i0 += 32 * kCopyIlp) {
+        size_t src[kCopyIlp];
+        uint32_t val[kCopyIlp];
+#pragma unroll
+        for (uint32_t u = 0; u < kCopyIlp; ++u) {
+            const uint32_t i = i0 + u * 32 + lane;
+            uint32_t q = 0;  // the last cluster whose exclusive sum is <= i (lanes past the group hold `total`)
+#pragma unroll
+            for (uint32_t step = 16; step; step >>= 1) {
+                const uint32_t e = __shfl_sync(kFull, excl, q + step);
+                if (e <= i) q += step;
+            }
+            const uint32_t eq = __shfl_sync(kFull, excl, q);
+            src[u] = (size_t)(first + q) * v.cap + (i - eq);
+        }
+#pragma unroll
+        for (uint32_t u = 0; u < kCopyIlp; ++u) val[u] = i0 + u * 32 + lane < total ? __ldg(&v.staging[src[u]]) : 0u;
+#pragma unroll
+        for (uint32_t u = 0; u < kCopyIlp; ++u)
+            if (i0 + u * 32 + lane < total) v.indices[base + i0 + u * 32 + lane] = val[u];
     }
-    const uint32_t cj = first + lane;
-    const uint32_t before = warp_sum(cj < c ? v.counts[cj] : 0u);
-    const uint32_t n = v.counts[c];
-    const uint32_t offset = v.group_offsets[b] + before;
-    if (lane == 0) v.cells[c] = CfLightCell{offset, n};
-    const uint32_t* src = v.staging + (size_t)c * v.cap;
-    for (uint32_t i = lane; i < n; i += 32) v.indices[offset + i] = src[i];
 }
 
 __global__ void __launch_bounds__(kCopyWarps * 32) copy_kernel(const ViewCull v)
@@ -980,14 +1353,36 @@ template <int K, int WARPS, int TILE, int STAGES, bool kBinned>
 cudaError_t launch_cull_t(const ViewCull& v, uint32_t* dev_error, cudaStream_t stream)
 {
     static_assert(WARPS * K <= 32, "a cluster group fits one warp of the copy kernel");
-    const size_t smem = CullSmem<K, WARPS, TILE, STAGES, kBinned>::bytes();
-    if (smem > 48 * 1024) {  // opt in above the default 48 KB (a per-device attribute)
-        const cudaError_t e = cudaFuncSetAttribute(cull_kernel<K, WARPS, TILE, STAGES, kBinned>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
+    if constexpr (kBinned) {
+        // one persistent CTA per resident slot, taking the view's groups in order
+        const size_t psmem = PipeSmem<K, WARPS, TILE, STAGES>::bytes;
+        static const int resident = [psmem] {  // thread-safe one-time query
+            int dev = 0, sms = 0, b = 0;
+            cudaError_t e = cudaGetDevice(&dev);
+            if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e == cudaSuccess && psmem > 48 * 1024)
+                e = cudaFuncSetAttribute(cull_pipe_kernel<K, WARPS, TILE, STAGES>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem);
+            if (e == cudaSuccess)
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, cull_pipe_kernel<K, WARPS, TILE, STAGES>,
+                                                                  (WARPS + 1) * 32, psmem);
+            return e == cudaSuccess ? sms * (b > 0 ? b : 1) : 0;
+        }();
+        if (resident <= 0) return cudaErrorInvalidConfiguration;
+        const uint32_t ctas = std::min<uint32_t>(v.groups, (uint32_t)resident);
+        cull_pipe_kernel<K, WARPS, TILE, STAGES>
+            <<<ctas, (WARPS + 1) * 32, psmem, stream>>>(nullptr, nullptr, v.groups, v.queue, dev_error, v);
+        return cudaGetLastError();
+    } else {
+        const size_t smem = CullSmem<K, WARPS, TILE, STAGES, kBinned>::bytes();
+        if (smem > 48 * 1024) {  // opt in above the default 48 KB (a per-device attribute)
+            const cudaError_t e = cudaFuncSetAttribute(cull_kernel<K, WARPS, TILE, STAGES, kBinned>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        cull_kernel<K, WARPS, TILE, STAGES, kBinned><<<v.groups, (WARPS + 1) * 32, smem, stream>>>(v, dev_error);
+        return cudaGetLastError();
     }
-    cull_kernel<K, WARPS, TILE, STAGES, kBinned><<<v.groups, (WARPS + 1) * 32, smem, stream>>>(v, dev_error);
-    return cudaGetLastError();
 }
 
 }  // namespace
@@ -1085,7 +1480,7 @@ cudaError_t launch_light_xform(const CfLightData* lights, uint32_t count, const 
 cudaError_t launch_bin(const ViewCull& v, cudaStream_t stream)
 {
     if (v.slices == 0) return cudaSuccess;
-    bin_slices_kernel<<<v.slices, kBinWarps * 32, 0, stream>>>(v);
+    bin_slices_kernel<<<(v.slices + kBinSlicesSingle - 1) / kBinSlicesSingle, kBinWarpsSingle * 32, 0, stream>>>(v);
     return cudaGetLastError();
 }
 
@@ -1109,7 +1504,7 @@ cudaError_t launch_finalize(const ViewCull& v, cudaStream_t stream)
     scan_kernel<<<1, kScanThreads, 0, stream>>>(v);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    copy_kernel<<<(v.clusters + kCopyWarps - 1) / kCopyWarps, kCopyWarps * 32, 0, stream>>>(v);
+    copy_kernel<<<copy_blocks(v.groups), kCopyWarps * 32, 0, stream>>>(v);
     return cudaGetLastError();
 }
 
@@ -1210,27 +1605,36 @@ cudaError_t launch_batch_aabb(const AabbJob* jobs, const uint32_t* prefix, uint3
 // ---------------------------------------------------------------------------
 namespace {
 
+// Batches are always binned: a plain configuration has no batched kernel.
 template <int K, int WARPS, int TILE, int STAGES, bool kBinned>
 cudaError_t launch_cull_batch_t(const BatchCull& b, int ctas, uint32_t* dev_error, cudaStream_t stream)
 {
     static_assert(WARPS * K <= 32, "a cluster group fits one warp of the copy kernel");
-    const size_t smem = CullSmem<K, WARPS, TILE, STAGES, kBinned>::bytes();
-    if (smem > 48 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(cull_batch_kernel<K, WARPS, TILE, STAGES, kBinned>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
+    if constexpr (!kBinned) {
+        return cudaErrorInvalidValue;
+    } else {
+        const size_t smem = PipeSmem<K, WARPS, TILE, STAGES>::bytes;
+        if (smem > 48 * 1024) {
+            const cudaError_t e = cudaFuncSetAttribute(cull_pipe_kernel<K, WARPS, TILE, STAGES>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        cull_pipe_kernel<K, WARPS, TILE, STAGES>
+            <<<ctas, (WARPS + 1) * 32, smem, stream>>>(b.jobs, b.items, b.n_items, b.queue, dev_error, ViewCull{});
+        return cudaGetLastError();
     }
-    cull_batch_kernel<K, WARPS, TILE, STAGES, kBinned>
-        <<<ctas, (WARPS + 1) * 32, smem, stream>>>(b.jobs, b.items, b.n_items, b.queue, dev_error);
-    return cudaGetLastError();
 }
 
 template <int K, int WARPS, int TILE, int STAGES, bool kBinned>
 cudaError_t batch_occupancy_t(int* blocks)
 {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, cull_batch_kernel<K, WARPS, TILE, STAGES, kBinned>,
-                                                         (WARPS + 1) * 32,
-                                                         CullSmem<K, WARPS, TILE, STAGES, kBinned>::bytes());
+    if constexpr (!kBinned) {
+        *blocks = 0;
+        return cudaErrorInvalidValue;
+    } else {
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, cull_pipe_kernel<K, WARPS, TILE, STAGES>,
+                                                             (WARPS + 1) * 32, PipeSmem<K, WARPS, TILE, STAGES>::bytes);
+    }
 }
 
 }  // namespace
@@ -1249,7 +1653,7 @@ cudaError_t launch_batch_bin(const ViewJob* jobs, const uint32_t* prefix, uint32
                              cudaStream_t stream)
 {
     if (blocks == 0) return cudaSuccess;
-    batch_bin_kernel<<<blocks, kBinWarps * 32, 0, stream>>>(jobs, prefix, n_views);
+    batch_bin_kernel<<<blocks, kBinWarpsBatch * 32, 0, stream>>>(jobs, prefix, n_views);
     return cudaGetLastError();
 }
 
@@ -1296,6 +1700,7 @@ cudaError_t launch_batch_copy(const ViewJob* jobs, const uint32_t* prefix, uint3
     return cudaGetLastError();
 }
 
-uint32_t copy_blocks(uint32_t clusters) { return (clusters + kCopyWarps - 1) / kCopyWarps; }
+uint32_t copy_blocks(uint32_t groups) { return (groups + kCopyWarps - 1) / kCopyWarps; }
+uint32_t bin_blocks(uint32_t slices) { return (slices + kBinSlicesBatch - 1) / kBinSlicesBatch; }
 
 }  // namespace cfk

@@ -11,10 +11,11 @@
 //                                          light whose view-space position is not
 //                                          finite (those granules take the exact
 //                                          branchy test)
-//   counts    C x uint32                   capped hit count per cluster
+//   counts    C x uint32                   capped hit count per cluster (plain path)
 //   staging   C x cap x uint32             each cluster's hits in ascending order
 //   cells     C x CfLightCell              output
 //   indices   >= sum(counts) x uint32      output, packed in cluster order
+// and, on the binned path, per depth slice a candidate list (slice_*).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -56,8 +57,9 @@ struct ViewCull {
     // cluster groups: the clusters one culling CTA owns.  Plain: group b is
     // [b*gw, min((b+1)*gw, C)); binned: group b is slice b / gps, clusters
     // [k*XY + (b % gps)*gw, min(.. + gw, (k+1)*XY)).
-    uint32_t* group_sums;     // capped hit count of each group
-    uint32_t* group_offsets;  // exclusive scan of group_sums
+    uint32_t* group_sums;     // capped hit count of each group (plain path)
+    uint32_t* group_offsets;  // exclusive scan of group_sums (plain path)
+    uint32_t* queue;          // single-view binned launch: item counter, zeroed by the binning launch
     uint32_t lpad;
     uint32_t clusters;
     uint32_t cap;
@@ -114,6 +116,7 @@ struct WorkspaceLayout {
     size_t vlights, nonfinite, counts, staging, group_sums, group_offsets, slice_lights, slice_idx, slice_count,
         slice_nonfinite, bytes;
 };
+constexpr size_t kQueueWord = 64;  // byte offset, in a workspace's status block, of the single-view item counter
 // Scratch of one view; `groups` = group_count(...) of the configuration used.
 WorkspaceLayout workspace_layout(uint32_t clusters, uint32_t lights, uint32_t cap, uint32_t slices, bool binned,
                                  uint32_t groups);
@@ -163,6 +166,7 @@ cudaError_t batch_cull_resident_ctas(const CullConfig& cfg, int* ctas);
 cudaError_t launch_batch_scan(const ViewJob* jobs, uint32_t n_views, cudaStream_t stream);
 cudaError_t launch_batch_copy(const ViewJob* jobs, const uint32_t* prefix, uint32_t n_views, uint32_t blocks,
                               cudaStream_t stream);
-uint32_t copy_blocks(uint32_t clusters);
+uint32_t copy_blocks(uint32_t groups);  // blocks of the copy launch for a view of `groups` cluster groups
+uint32_t bin_blocks(uint32_t slices);   // blocks of a batched binning launch for a view of `slices` depth slices
 
 }  // namespace cfk

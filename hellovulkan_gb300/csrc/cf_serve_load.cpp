@@ -224,6 +224,14 @@ extern "C" int cf_serve_run_load(CfServer* server, const CfServeLoad* load, CfSe
     rep.jitter_call_p99_us = percentile(jit_us, 0.99);
     rep.submit_call_p50_us = percentile(sub_us, 0.50);
     rep.submit_call_p99_us = percentile(sub_us, 0.99);
+    auto vmax = [](const std::vector<double>& v) { return v.empty() ? 0.0 : *std::max_element(v.begin(), v.end()); };
+    rep.register_call_max_us = vmax(reg_us);
+    rep.jitter_call_max_us = vmax(jit_us);
+    rep.submit_call_max_us = vmax(sub_us);
+    size_t worst = 0;
+    for (size_t i = 1; i < n; ++i)
+        if (submit_lag[i] > submit_lag[worst]) worst = i;
+    rep.worst_lag_arrival_s = n ? arrival[worst] : 0.0;
     rep.tests_brute_force = tests_done;
     *report = rep;
     return CF_SUCCESS;

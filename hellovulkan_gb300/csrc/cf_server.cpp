@@ -435,8 +435,8 @@ void plan_batch(CfServer* s, int slot_i, const std::vector<Request*>& reqs, Laun
         prefix[n + i] = bb;
         prefix[2 * n + i] = cb;
         xb += cfk::granules(j.v.lpad);
-        bb += j.v.slices;
-        cb += cfk::copy_blocks(r->clusters);
+        bb += cfk::bin_blocks(j.v.slices);
+        cb += cfk::copy_blocks(r->groups);
         buckets[j.v.slice_clusters].push_back(i);
     }
     uint32_t ni = 0;

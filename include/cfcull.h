@@ -354,6 +354,8 @@ typedef struct CfServeReport {
     double register_call_p50_us, register_call_p99_us;  /* time inside cf_server_register_light_set */
     double jitter_call_p50_us, jitter_call_p99_us;      /* time inside cf_server_jitter_light_set   */
     double submit_call_p50_us, submit_call_p99_us;      /* time inside cf_server_submit             */
+    double register_call_max_us, jitter_call_max_us, submit_call_max_us;
+    double worst_lag_arrival_s;                         /* scheduled arrival of the most delayed submit */
 } CfServeReport;
 
 CFCULL_API int cf_serve_run_load(CfServer* server, const CfServeLoad* load, CfServeReport* report);

@@ -526,6 +526,7 @@ def run_ours(args):
     aabb_ms = e0.elapsed_time(e1)
 
     cull.set_cluster_forward_ubo(view.ubo)
+    cull_cfg_used = cull.tuning()
     cull.enable_stage_timing(True)
 
     def timed_steps(n):
@@ -652,10 +653,13 @@ def run_ours(args):
     H = o_idx.size
     cull_ops = (work_filter + work_cluster) * OPS_PER_TEST
     fin_bytes = 12 * view.clusters + 8 * H
+    auto_cfg = cull_cfg_used
+    cull_kernel_name = ("bin_slices_kernel + cull_pipe_kernel<%d,%d,%d,%d> (binned)" if auto_cfg[4] else
+                        "cull_kernel<%d,%d,%d,%d> (brute force)") % tuple(auto_cfg[:4])
     if st_c >= st_f:
         ach = cull_ops / (st_c * 1e-3) / 1e12
         roof = {"bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "Tops/s", "frac": ach / fp32_peak,
-                "traffic": traffic.get("cull"), "kernel": "bin_slices_kernel + cull_kernel (binned)",
+                "traffic": traffic.get("cull"), "kernel": cull_kernel_name,
                 "ops_per_launch": cull_ops, "peak_source": peak_note,
                 "work": "executed sphere-box tests x %d ops (work counters): %d slab/union + %d cluster" % (
                     OPS_PER_TEST, work_filter, work_cluster)}

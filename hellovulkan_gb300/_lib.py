@@ -203,6 +203,7 @@ _SIGS = {
     "cf_pipeline_light_culling_set_cluster_forward_ubo": [_P, C.POINTER(CfClusterForwardUBO)],
     "cf_pipeline_light_culling_fill_command_buffer": [_P, _P],
     "cf_pipeline_light_culling_set_tuning": [_P, _I, _I, _I, _I, _I],
+    "cf_pipeline_light_culling_get_tuning": [_P, C.POINTER(_I)],
     "cf_pipeline_light_culling_enable_stage_timing": [_P, _I],
     "cf_pipeline_light_culling_get_stage_times": [_P, C.POINTER(C.c_float)],
     "cf_pipeline_light_culling_enable_work_counters": [_P, _I],

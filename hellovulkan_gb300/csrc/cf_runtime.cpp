@@ -680,6 +680,19 @@ int cf_pipeline_light_culling_set_tuning(CfPipelineLightCulling* p, int clusters
     return CF_SUCCESS;
 }
 
+int cf_pipeline_light_culling_get_tuning(const CfPipelineLightCulling* p, int config[5])
+{
+    if (!p || !config) return fail(CF_ERROR_INVALID_ARGUMENT, "null argument");
+    if (!p->has_ubo || !p->lights) return fail(CF_ERROR_NOT_READY, "no cluster-forward UBO set yet");
+    const cfk::CullConfig c = choose_config(p->ubo, p->lights->count, p->has_cfg ? &p->cfg : nullptr);
+    config[0] = c.clusters_per_warp;
+    config[1] = c.warps;
+    config[2] = c.tile;
+    config[3] = c.stages;
+    config[4] = c.binned;
+    return CF_SUCCESS;
+}
+
 // --- stateless -------------------------------------------------------------
 int cf_cull_workspace_device_error(void* d_workspace, uint32_t* device_error)
 {

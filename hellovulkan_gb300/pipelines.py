@@ -169,6 +169,12 @@ class PipelineLightCulling:
     def fill_command_buffer(self, stream=None) -> None:
         check(lib().cf_pipeline_light_culling_fill_command_buffer(self.handle, stream_handle(stream)))
 
+    def tuning(self):
+        """(clusters_per_warp, warps, tile, stages, binned) the next fill uses."""
+        out = (C.c_int * 5)()
+        check(lib().cf_pipeline_light_culling_get_tuning(self.handle, out))
+        return tuple(out)
+
     def enable_stage_timing(self, enable: bool = True) -> None:
         check(lib().cf_pipeline_light_culling_enable_stage_timing(self.handle, int(enable)))
 

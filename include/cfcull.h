@@ -181,6 +181,10 @@ CFCULL_API int cf_pipeline_light_culling_fill_command_buffer(CfPipelineLightCull
  * output. */
 CFCULL_API int cf_pipeline_light_culling_set_tuning(CfPipelineLightCulling* pipe, int clusters_per_warp, int warps,
                                                     int tile, int stages, int binned);
+/* The configuration the next fill_command_buffer uses (the override, or the
+ * automatic choice for the current UBO and light count): clusters per warp,
+ * warps, tile, stages, binned. */
+CFCULL_API int cf_pipeline_light_culling_get_tuning(const CfPipelineLightCulling* p, int config[5]);
 /* Stage timing, the counterpart of the reference's Tracy GPU zone
  * "Light_Culling" (PipelineLightCulling.cpp:53): when enabled, each
  * fill_command_buffer records CUDA events around its three kernels, and

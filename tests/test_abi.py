@@ -64,12 +64,17 @@ def test_status_strings_and_argument_errors_without_gpu(cflib):
     from hellovulkan_gb300 import scenes
     v = scenes.plain_small(1)
     assert L.cf_cull_workspace_size(C.byref(v.ubo), 1024, 150, C.byref(n)) == 0
-    # status block + lights + flags + counts + staging + group sums and offsets
-    # (24 slices x 9 groups of 16 clusters) + 24 slice candidate lists
-    # (float4 + index) + slice counts + slice flags, each 256-byte aligned
+    # 3.5 M tests: brute force.  Status block + lights + flags + counts +
+    # staging + group sums and offsets (432 groups of 8 clusters), each
+    # 256-byte aligned
     al = lambda x: (x + 255) // 256 * 256
-    assert n.value == (256 + al(1024 * 16) + al(4 * 4) + al(3456 * 4) + al(3456 * 150 * 4) + 2 * al(216 * 4)
-                       + al(24 * 1024 * 16) + al(24 * 1024 * 4) + 2 * al(24 * 4))
+    assert n.value == (256 + al(1024 * 16) + al(4 * 4) + al(3456 * 4) + al(3456 * 150 * 4) + 2 * al(432 * 4))
+    big = scenes.plain_large(2)
+    assert L.cf_cull_workspace_size(C.byref(big.ubo), 16384, 150, C.byref(n)) == 0
+    # 453 M tests: binned, 48 slices x 36 groups of 16 clusters, plus 48 slice
+    # candidate lists (float4 + index), slice counts and slice flags
+    assert n.value == (256 + al(16384 * 16) + al(64 * 4) + al(27648 * 4) + al(27648 * 150 * 4) + 2 * al(1728 * 4)
+                       + al(48 * 16384 * 16) + al(48 * 16384 * 4) + 2 * al(48 * 4))
     ubo = _lib.CfClusterForwardUBO()
     ubo.sliceCountX, ubo.sliceCountY, ubo.sliceCountZ = 0, 9, 24
     assert L.cf_generate_aabbs(C.byref(ubo), C.c_void_p(256), None) == 1

@@ -444,6 +444,27 @@ def measure_lookup(ctx, stream, reps=20):
     s = samples_to_numpy(out, h, w)
     f = s["flags"]
     explained = (f & (FRAGMENT_OUTSIDE_AABB | FRAGMENT_CAPPED)) > 0
+
+    # Scene.frag's direct clustered lighting over a 1920x1080 G-buffer
+    from hellovulkan_gb300._lib import CfPBRPushConstant
+    from hellovulkan_gb300.consumer import shade_clusters
+    pc = CfPBRPushConstant(1.75, 0.01, 0.0, 0.1, 0.1)
+    g = torch.from_numpy(scenes.gbuffer(np.random.default_rng(8), v.ubo)).cuda()
+    cam = scenes.camera_position(v.ubo)
+
+    def shade():
+        return shade_clusters(v.ubo, cam, pc, g, b.light_cells, b.light_indices, idx.size, rl.device_buffer,
+                              v.light_count, stream)
+
+    for _ in range(3):
+        shade()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for a, c in ev:
+        a.record(stream)
+        shade()
+        c.record(stream)
+    torch.cuda.synchronize()
+    shade_ms = float(np.median([a.elapsed_time(c) for a, c in ev]))
     for o in (cu, gen, rc, rl):
         o.close()
     moved = w * h * (4 + 32)  # depth read + sample written; cells, indices and lights come from L2
@@ -453,7 +474,61 @@ def measure_lookup(ctx, stream, reps=20):
             "mean_covering_lights": float(s["covering"].mean()),
             "pixels_outside_their_box": int((f & FRAGMENT_OUTSIDE_AABB > 0).sum()),
             "pixels_missing_a_light": int((s["missing"] > 0).sum()),
-            "unexplained_misses": int(((s["missing"] > 0) & ~explained).sum())}
+            "unexplained_misses": int(((s["missing"] > 0) & ~explained).sum()),
+            "shading": {"workload": "1920x1080 G-buffer, direct clustered lighting (Radiance.glsl) over the culled "
+                                    "lists", "ms": shade_ms, "texels_per_s": w * h / (shade_ms * 1e-3),
+                        "gbs_gbuffer_and_output": w * h * (48 + 16) / (shade_ms * 1e-3) / 1e9}}
+
+
+def measure_frustum(stream, reps=50):
+    """FrustumCulling.comp (cf_frustum_cull) on 10 000 random boxes, the case
+    the reference's README quotes (under 25 microseconds on an RTX 3070
+    Mobile, whole dispatch), and on 16 M boxes (768 MB of boxes and commands,
+    larger than L2), whose cost is HBM traffic: 32 bytes read + 4 written per
+    box.  Checked against the oracle on the 10 000-box case."""
+    import math
+
+    import torch
+
+    from hellovulkan_gb300 import scenes
+    from hellovulkan_gb300.camera import frustum_ubo
+    from hellovulkan_gb300.consumer import frustum_cull
+    from oracle import Oracle
+    rng = np.random.default_rng(11)
+    f = frustum_ubo(math.radians(45.0), 16.0 / 9.0, 0.1, 500.0, scenes.random_camera(rng))
+    peaks = {}
+    try:
+        peaks = json.loads((REPO / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    out = {}
+    for n in (10000, 16 << 20):
+        boxes = torch.from_numpy(scenes.random_boxes(rng, n)).cuda()
+        cmds = torch.zeros((n, 4), dtype=torch.int32, device="cuda")
+        for _ in range(3):
+            frustum_cull(f, boxes, cmds, None, stream)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for a, c in ev:
+            a.record(stream)
+            frustum_cull(f, boxes, cmds, None, stream)
+            c.record(stream)
+        torch.cuda.synchronize()
+        ms = float(np.median([a.elapsed_time(c) for a, c in ev]))
+        r = {"boxes": n, "us": ms * 1e3, "boxes_per_s": n / (ms * 1e-3),
+             "kept": float(cmds[:, 1].float().mean().item())}
+        if n == 10000:
+            r["parity_with_oracle"] = bool(np.array_equal(cmds[:, 1].cpu().numpy().astype(np.uint32),
+                                                          Oracle().frustum_cull(f, boxes.cpu().numpy())))
+            r["reference_published_us"] = 25.0
+            r["reference_hardware"] = "RTX 3070 Mobile, 'less than 25 microseconds' (README.md:63)"
+        else:
+            gbs = n * 36 / (ms * 1e-3) / 1e9
+            r["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                             "bytes_per_launch": n * 36, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
+        out["boxes_%d" % n] = r
+        del boxes, cmds
+    return out
 
 
 def measure_stress(ctx, stream, n_views, n_lights, frames, seed=5):
@@ -599,9 +674,10 @@ def run_ours(args):
     batched = None
     if not args.no_batch and rank == 0:
         batched = measure_batch(ctx, stream)
-    lookup = None
+    lookup = frustum = None
     if rank == 0:
         lookup = measure_lookup(ctx, stream)
+        frustum = measure_frustum(stream)
     stress = None
     if not args.no_stress and rank == 0:
         stress = measure_stress(ctx, stream, args.stress_views, args.stress_lights, args.stress_frames)
@@ -717,6 +793,7 @@ def run_ours(args):
         "served": served,
         "stress": stress,
         "cluster_lookup": lookup,
+        "frustum_culling": frustum,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:

@@ -43,6 +43,15 @@ FRAGMENT_DTYPE = np.dtype([("cluster", "<u4"), ("offset", "<u4"), ("count", "<u4
 FRAGMENT_OUTSIDE_GRID, FRAGMENT_OUTSIDE_AABB, FRAGMENT_CAPPED, FRAGMENT_BAD_CELL = 1, 2, 4, 8
 
 
+class CfPBRPushConstant(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("lightIntensity", "baseReflectivity", "maxReflectionLod", "lightFalloff",
+                                         "albedoMultipler")]
+
+
+class CfFrustum(C.Structure):
+    _fields_ = [("planes", (C.c_float * 4) * 6), ("corners", (C.c_float * 4) * 8)]
+
+
 class CfClusterForwardUBO(C.Structure):
     _fields_ = [
         ("cameraInverseProjection", C.c_float * 16),
@@ -148,6 +157,7 @@ assert C.sizeof(CfServeLoad) == 128 and C.sizeof(CfServeReport) == 240
 assert CfServeLoad.projections.offset == 56 and CfServeLoad.eye_lo.offset == 80
 assert C.sizeof(CfBatchView) == 240 and C.sizeof(CfBatchInfo) == 216
 assert C.sizeof(CfLightData) == 48 and C.sizeof(CfAABB) == 32 and C.sizeof(CfLightCell) == 8
+assert C.sizeof(CfPBRPushConstant) == 20 and C.sizeof(CfFrustum) == 224
 assert C.sizeof(CfLightOrbit) == 32 and C.sizeof(CfFragmentSample) == 32 == FRAGMENT_DTYPE.itemsize
 assert C.sizeof(CfClusterForwardUBO) == 176
 
@@ -211,6 +221,9 @@ _SIGS = {
     "cf_cull_workspace_size": [C.POINTER(CfClusterForwardUBO), _U32, _U32, _PU64],
     "cf_generate_aabbs": [C.POINTER(CfClusterForwardUBO), _P, _P],
     "cf_animate_light_orbits": [_P, _P, _U64, _U32, _P],
+    "cf_shade_clusters": [C.POINTER(CfClusterForwardUBO), C.POINTER(C.c_float), C.POINTER(CfPBRPushConstant), _P, _U32,
+                          _U32, _P, _P, _U64, _P, _U32, _P, _P],
+    "cf_frustum_cull": [C.POINTER(CfFrustum), _P, _U32, _P, _P, _P],
     "cf_lookup_clusters": [C.POINTER(CfClusterForwardUBO), _P, _U32, _U32, _P, _P, _U64, _P, _U32, _U32, _P, _I, _P,
                            _P],
     "cf_cull_lights": [C.POINTER(CfClusterForwardUBO), _P, _P, _U32, _U32, _P, _P, _U64, _P, _P, _U64, _P],

@@ -91,3 +91,26 @@ def ubo_from_bytes(b) -> CfClusterForwardUBO:
 
 def ubo_grid(u: CfClusterForwardUBO):
     return int(u.sliceCountX), int(u.sliceCountY), int(u.sliceCountZ)
+
+
+def frustum_ubo(fovy: float, aspect: float, near: float, far: float, view: np.ndarray):
+    """Camera::GetFrustumUBO (Source/Camera.cpp:199-230): with PV = P * V (P
+    with the Vulkan y flip), the planes are row 3 +/- rows 0, 1, 2 of PV (left,
+    right, bottom, top, near, far) and the corners are the clip cube's
+    (+/-1, +/-1, +/-1) unprojected by inverse(PV) and divided by w.  Computed in
+    float64 and stored as float32 (the kernel and the oracle read the same
+    bytes, so the rounding here does not affect parity)."""
+    from ._lib import CfFrustum
+    P = perspective_rh_zo(fovy, aspect, near, far).astype(np.float64)
+    P[1, 1] *= -1.0
+    PV = P @ np.asarray(view, np.float64)
+    planes = [PV[3] + PV[0], PV[3] - PV[0], PV[3] + PV[1], PV[3] - PV[1], PV[3] + PV[2], PV[3] - PV[2]]
+    inv = np.linalg.inv(PV)
+    ndc = [(-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1), (-1, -1, 1), (1, -1, 1), (1, 1, 1), (-1, 1, 1)]
+    f = CfFrustum()
+    for i, p in enumerate(planes):
+        f.planes[i][:] = [float(np.float32(x)) for x in p]
+    for i, c in enumerate(ndc):
+        q = inv @ np.array([c[0], c[1], c[2], 1.0])
+        f.corners[i][:] = [float(np.float32(x)) for x in q / q[3]]
+    return f

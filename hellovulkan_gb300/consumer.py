@@ -1,6 +1,8 @@
-"""The consumer side of the culled lists (include/cfcull.h, cf_lookup_clusters).
+"""The consumer side of the culled lists (include/cfcull.h, cf_lookup_clusters,
+cf_shade_clusters).
 
-    samples = lookup_clusters(ubo, depth, cells, indices, lights, index_count)
+    samples = lookup_clusters(ubo, depth, cells, indices, lights, index_count, light_count)
+    rgba = shade_clusters(ubo, camera_position, pc, gbuffer, cells, indices, index_count, lights, light_count)
 
 Scene.frag's per-fragment cluster lookup (HelloVulkan/Shaders/ClusteredForward/
 Scene.frag:54-78) run on the GPU over a depth buffer: which cluster each pixel
@@ -33,3 +35,29 @@ def lookup_clusters(ubo, depth, cells, indices, lights, index_count: int, light_
 
 def samples_to_numpy(out, height: int, width: int) -> np.ndarray:
     return out.cpu().numpy().view(FRAGMENT_DTYPE).reshape(height, width)
+
+
+def shade_clusters(ubo, camera_position, pc, gbuffer, cells, indices, index_count: int, lights, light_count: int,
+                   stream=None):
+    """gbuffer: (h, w, 12) float32 device tensor of CfGBufferTexel records;
+    returns an (h, w, 4) float32 device tensor (Lo, alpha) — Scene.frag's
+    direct clustered lighting over the culled lists."""
+    import ctypes as C
+
+    import torch
+    h, w = int(gbuffer.shape[0]), int(gbuffer.shape[1])
+    out = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    addr = lambda t: None if t is None else (t if isinstance(t, int) else t.data_ptr())  # noqa: E731
+    cam = (C.c_float * 3)(*[float(v) for v in camera_position[:3]])
+    check(lib().cf_shade_clusters(C.byref(ubo), cam, C.byref(pc), addr(gbuffer), w, h, addr(cells), addr(indices),
+                                  index_count, addr(lights), light_count, out.data_ptr(), stream_handle(stream)))
+    return out
+
+
+def frustum_cull(frustum, boxes, commands, visible=None, stream=None) -> None:
+    """FrustumCulling.comp over device tensors: boxes (n, 8) float32 AABBs,
+    commands (n, 4) uint32/int32 VkDrawIndirectCommand records whose
+    instanceCount is set to 0 or 1; visible: optional one-element counter."""
+    import ctypes as C
+    check(lib().cf_frustum_cull(C.byref(frustum), boxes.data_ptr(), int(boxes.shape[0]), commands.data_ptr(),
+                                None if visible is None else visible.data_ptr(), stream_handle(stream)))

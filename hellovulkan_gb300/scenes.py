@@ -205,3 +205,53 @@ def depth_log_uniform(rng: np.random.Generator, width: int, height: int, near: f
     if far_plane_fraction > 0:
         z[rng.uniform(size=z.shape) < far_plane_fraction] = 1.0
     return z
+
+
+def camera_position(ubo) -> np.ndarray:
+    """World-space eye position of a UBO's view matrix (float64)."""
+    view = np.array(list(ubo.cameraView), np.float64).reshape(4, 4).T
+    return np.linalg.inv(view)[:3, 3]
+
+
+def gbuffer(rng: np.random.Generator, ubo, far_plane_fraction: float = 0.0) -> np.ndarray:
+    """A synthetic (height, width, 12) float32 G-buffer of CfGBufferTexel
+    records for the UBO's screen: log-uniform linear depths, each texel's world
+    position unprojected from its pixel centre and depth, a random unit normal
+    facing the camera, albedo U[0,1]^3, metallic U[0,1], roughness U[0.05,1]."""
+    w, h = int(ubo.screenSize[0]), int(ubo.screenSize[1])
+    z = depth_log_uniform(rng, w, h, float(ubo.cameraNear), float(ubo.cameraFar), far_plane_fraction)
+    inv_p = np.array(list(ubo.cameraInverseProjection), np.float64).reshape(4, 4).T
+    view = np.array(list(ubo.cameraView), np.float64).reshape(4, 4).T
+    xs = (np.arange(w) + 0.5) / w * 2.0 - 1.0
+    ys = (np.arange(h) + 0.5) / h * 2.0 - 1.0
+    clip = np.stack([np.broadcast_to(xs[None, :], (h, w)), np.broadcast_to(ys[:, None], (h, w)),
+                     z.astype(np.float64), np.ones((h, w))], axis=-1)
+    v = clip @ inv_p.T
+    v = v / v[..., 3:4]
+    world = v @ np.linalg.inv(view).T
+    eye = camera_position(ubo)
+    n = rng.normal(size=(h, w, 3))
+    n /= np.linalg.norm(n, axis=-1, keepdims=True)
+    to_eye = eye - world[..., :3]
+    n = np.where((np.sum(n * to_eye, axis=-1) < 0)[..., None], -n, n)
+    out = np.empty((h, w, 12), np.float32)
+    out[..., 0:3] = world[..., :3]
+    out[..., 3] = z
+    out[..., 4:7] = n
+    out[..., 7] = rng.uniform(0.0, 1.0, (h, w))
+    out[..., 8:11] = rng.uniform(0.0, 1.0, (h, w, 3))
+    out[..., 11] = rng.uniform(0.05, 1.0, (h, w))
+    return out
+
+
+def random_boxes(rng: np.random.Generator, n: int, extent: float = 200.0, size_lo: float = 0.5,
+                 size_hi: float = 10.0) -> np.ndarray:
+    """n axis-aligned boxes (CfAABB records, (n, 8) float32, w = 0) with
+    centres uniform in [-extent, extent]^3 and sides uniform in
+    [size_lo, size_hi] — the objects of a frustum-culling scene."""
+    c = rng.uniform(-extent, extent, size=(n, 3))
+    h = rng.uniform(size_lo, size_hi, size=(n, 3)) / 2.0
+    out = np.zeros((n, 8), np.float32)
+    out[:, 0:3] = c - h
+    out[:, 4:7] = c + h
+    return out

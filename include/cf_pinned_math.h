@@ -109,6 +109,16 @@ CF_HD float cf_fdiv(float a, float b)
 #endif
 }
 
+/* Correctly rounded square root (IEEE 754 requires it of sqrt). */
+CF_HD float cf_fsqrt(float a)
+{
+#if defined(__CUDA_ARCH__)
+    return __fsqrt_rn(a);
+#else
+    return __builtin_sqrtf(a);
+#endif
+}
+
 /* GLSL min / max (GLSL 4.60 §8.3). */
 CF_HD float cf_glsl_min(float x, float y) { return (y < x) ? y : x; }
 CF_HD float cf_glsl_max(float x, float y) { return (x < y) ? y : x; }

@@ -94,6 +94,42 @@ typedef struct CfFragmentSample {
 #define CF_FRAGMENT_BAD_CELL 8u      /* the cell points outside the index list, or an
                                         index is not a light: nothing read through it */
 
+/* The PBR push constants of the clustered-forward fragment pass, byte for
+ * byte (Shaders/PBR/PBRPushConstants.glsl:1-8, Header/PushConstants.h:22-29). */
+typedef struct CfPBRPushConstant {
+    float lightIntensity;
+    float baseReflectivity;
+    float maxReflectionLod;
+    float lightFalloff;
+    float albedoMultipler;
+} CfPBRPushConstant;
+
+/* One G-buffer texel for cf_shade_clusters: the inputs Scene.frag gathers per
+ * fragment (world position and window depth, the shading normal, linear
+ * albedo, metallic and roughness). */
+typedef struct CfGBufferTexel {
+    CF_ALIGNAS(16) float position[4]; /* world xyz, w = gl_FragCoord.z (0..1) */
+    float normal[4];                  /* unit normal xyz, w = metallic        */
+    float albedo[4];                  /* linear albedo rgb, w = roughness     */
+} CfGBufferTexel;
+
+/* The frustum of FrustumCulling.comp, byte for byte (Shaders/Frustum.glsl:1-5,
+ * Header/UBOs.h:91-98): six planes (left, right, bottom, top, near, far) as
+ * rows of projection * view, and the eight corners of the clip cube
+ * unprojected to world space. */
+typedef struct CfFrustum {
+    CF_ALIGNAS(16) float planes[6][4];
+    float corners[8][4];
+} CfFrustum;
+
+/* VkDrawIndirectCommand (Shaders/DrawIndirectCommand.glsl:1-7). */
+typedef struct CfDrawIndirectCommand {
+    uint32_t vertexCount;
+    uint32_t instanceCount;
+    uint32_t firstVertex;
+    uint32_t firstInstance;
+} CfDrawIndirectCommand;
+
 /* Per-view parameters, std140: invProj @0, view @64, screenSize @128,
  * sliceScaling @136, sliceBias @140, near @144, far @148, X/Y/Z @152/156/160.
  * 164 bytes are used; the C++ mirror in the reference is 176 bytes. */
@@ -126,6 +162,10 @@ static_assert(offsetof(CfLightCell, count) == 4, "LightCell.count @4");
 static_assert(sizeof(CfClusterForwardUBO) == 176, "ClusterForwardUBO C++ sizeof");
 static_assert(sizeof(CfLightOrbit) == 32 && offsetof(CfLightOrbit, center) == 16, "LightOrbit is two float4");
 static_assert(sizeof(CfFragmentSample) == 32, "FragmentSample is 32 bytes");
+static_assert(sizeof(CfPBRPushConstant) == 20, "PBRPushConstant is five floats");
+static_assert(sizeof(CfFrustum) == 224 && offsetof(CfFrustum, corners) == 96, "FrustumUBO layout");
+static_assert(sizeof(CfDrawIndirectCommand) == 16, "VkDrawIndirectCommand is four uint");
+static_assert(sizeof(CfGBufferTexel) == 48, "GBufferTexel is three float4");
 static_assert(offsetof(CfClusterForwardUBO, cameraView) == 64, "view @64");
 static_assert(offsetof(CfClusterForwardUBO, screenSize) == 128, "screenSize @128");
 static_assert(offsetof(CfClusterForwardUBO, sliceScaling) == 136, "sliceScaling @136");

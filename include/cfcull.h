@@ -403,6 +403,34 @@ CFCULL_API int cf_lookup_clusters(const CfClusterForwardUBO* ubo, const float* d
                                   uint64_t index_count, const CfLightData* d_lights, uint32_t light_count,
                                   uint32_t max_lights_per_cluster, const CfAABB* d_aabbs, int check_all_lights,
                                   CfFragmentSample* d_out, void* stream);
+/* Scene.frag's direct clustered lighting for every texel of a G-buffer:
+ * the cluster lookup of cf_lookup_clusters on the texel's depth and pixel,
+ * then Lo = albedo * albedoMultipler + the sum of Radiance(...)
+ * (Shaders/ClusteredForward/Radiance.glsl:2-57, Scene.frag:82-135) over the
+ * cluster's listed lights, with V = normalize(camera_position - world
+ * position) and F0 = mix(baseReflectivity, albedo, metallic).  The shader's
+ * implementation-defined parts are pinned: normalize(v) = v / sqrt(dot(v, v))
+ * and length = sqrt(dot) with the correctly rounded sqrt, dot summed x, y, z,
+ * pow = cf_pow_pinned, every operation rounded to nearest in the shader's
+ * order.  The ambient (IBL) and emissive terms, which need the engine's
+ * textures, are not part of this pass.  d_out receives width x height float4
+ * (Lo, 1); texels whose lookup leaves the grid or meets a bad cell get
+ * (albedo * albedoMultipler, 0).  d_gbuffer and d_lights 16-byte aligned. */
+CFCULL_API int cf_shade_clusters(const CfClusterForwardUBO* ubo, const float camera_position[3],
+                                 const CfPBRPushConstant* pc, const CfGBufferTexel* d_gbuffer, uint32_t width,
+                                 uint32_t height, const CfLightCell* d_cells, const uint32_t* d_indices,
+                                 uint64_t index_count, const CfLightData* d_lights, uint32_t light_count,
+                                 float* d_out, void* stream);
+/* FrustumCulling.comp (Shaders/FrustumCulling.comp:14-57) for count boxes:
+ * d_commands[i].instanceCount = 1 when box i may intersect the frustum (host
+ * pointer; no plane has all 8 box corners behind it and no box face has all
+ * 8 frustum corners beyond it), else 0; the other fields of the commands are
+ * left as they are.  dot(plane, corner) is summed x, y, z, w in order.
+ * d_visible (optional, device, zeroed by the caller) receives the number of
+ * boxes kept.  The counterpart of PipelineFrustumCulling::FillCommandBuffer
+ * (Source/Pipelines/PipelineFrustumCulling.cpp). */
+CFCULL_API int cf_frustum_cull(const CfFrustum* frustum, const CfAABB* d_boxes, uint32_t count,
+                               CfDrawIndirectCommand* d_commands, uint32_t* d_visible, void* stream);
 /* LightCulling.comp: d_cells[C] and d_indices (capacity >= C * cap) from
  * d_aabbs[C] and d_lights[light_count]; d_total (optional, device) receives
  * the number of indices.  d_workspace: >= cf_cull_workspace_size bytes,

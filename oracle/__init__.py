@@ -39,6 +39,9 @@ class Oracle:
         L.cfo_exp2.argtypes = [C.c_float]
         L.cfo_lookup_clusters.argtypes = [_P, _P, C.c_uint32, C.c_uint32, _P, _P, C.c_uint64, _P, C.c_uint32,
                                           C.c_uint32, _P, C.c_int, _P, C.c_int]
+        L.cfo_shade_clusters.argtypes = [_P, _P, _P, _P, C.c_uint32, C.c_uint32, _P, _P, C.c_uint64, _P, C.c_uint32,
+                                         _P, C.c_int]
+        L.cfo_frustum_cull.argtypes = [_P, _P, C.c_uint32, _P, C.c_int]
         L.cfo_fp_contract_probe.argtypes = []
         L.cfo_max_threads.argtypes = []
         self.lib = L
@@ -83,6 +86,35 @@ class Oracle:
                                           lights.ctypes.data if lights.size else None, lights.shape[0], cap,
                                           None if ab is None else ab.ctypes.data, int(check_all), out.ctypes.data,
                                           threads)
+        assert st == 0, st
+        return out
+
+    def shade_clusters(self, ubo, camera_position, pc, gbuffer: np.ndarray, cells: np.ndarray, indices: np.ndarray,
+                       lights: np.ndarray, threads: int = 0) -> np.ndarray:
+        """Scene.frag's direct clustered lighting per G-buffer texel
+        (cfo_shade_clusters): gbuffer (h, w, 12) float32 CfGBufferTexel
+        records; returns (h, w, 4) float32 (Lo, alpha)."""
+        g = np.ascontiguousarray(gbuffer, np.float32)
+        h, w = g.shape[:2]
+        cells = np.ascontiguousarray(cells, np.uint32)
+        indices = np.ascontiguousarray(indices, np.uint32)
+        lights = np.ascontiguousarray(lights, np.float32).reshape(-1, 12)
+        cam = (C.c_float * 3)(*[float(v) for v in camera_position[:3]])
+        out = np.zeros((h, w, 4), np.float32)
+        st = self.lib.cfo_shade_clusters(_ubo_ptr(ubo), cam, C.byref(pc), g.ctypes.data, w, h, cells.ctypes.data,
+                                         indices.ctypes.data if indices.size else None, indices.size,
+                                         lights.ctypes.data if lights.size else None, lights.shape[0],
+                                         out.ctypes.data, threads)
+        assert st == 0, st
+        return out
+
+    def frustum_cull(self, frustum, boxes: np.ndarray, threads: int = 0) -> np.ndarray:
+        """FrustumCulling.comp per box (cfo_frustum_cull): the instanceCount
+        (0 or 1) of each box's draw command."""
+        b = np.ascontiguousarray(boxes, np.float32).reshape(-1, 8)
+        out = np.zeros(b.shape[0], np.uint32)
+        st = self.lib.cfo_frustum_cull(C.byref(frustum), b.ctypes.data if b.size else None, b.shape[0],
+                                       out.ctypes.data if out.size else None, threads)
         assert st == 0, st
         return out
 

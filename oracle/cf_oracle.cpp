@@ -12,6 +12,8 @@
  *   cfo_cull            HelloVulkan/Shaders/ClusteredForward/LightCulling.comp:26-87
  *   cfo_lookup_clusters HelloVulkan/Shaders/ClusteredForward/Scene.frag:54-78 (the consumer's
  *                       cluster lookup), a check of the culled lists
+ *   cfo_shade_clusters  Scene.frag:82-135 + Radiance.glsl:2-57 (direct clustered lighting)
+ *   cfo_frustum_cull    HelloVulkan/Shaders/FrustumCulling.comp:14-57
  *
  * with the three implementation-defined parts of GLSL pinned exactly as in
  * include/cf_pinned_math.h (pow, mat4*vec4 summation order, no FMA).  This
@@ -269,6 +271,141 @@ int cfo_lookup_clusters(const CfClusterForwardUBO* ubo, const float* depth, uint
             for (uint32_t i = 0; i < light_count; ++i)
                 if (!listed[i] && covers(i)) r.missing++;
         out[pix] = r;
+    }
+    return 0;
+}
+
+/*
+ * Scene.frag:82-135's direct clustered lighting per G-buffer texel (the
+ * lookup as in cfo_lookup_clusters), Radiance.glsl:2-57 and the PBRHeader.glsl
+ * helpers in their operation order, with normalize(v) = v / sqrt(dot(v, v)),
+ * length = sqrt(dot), pow = cf_pow_pinned (the pins cf_shade_clusters states).
+ * out: width x height x 4 floats.  Returns 0 or 1 (bad argument).
+ */
+int cfo_shade_clusters(const CfClusterForwardUBO* ubo, const float* cam, const CfPBRPushConstant* pc,
+                       const CfGBufferTexel* gbuf, uint32_t width, uint32_t height, const CfLightCell* cells,
+                       const uint32_t* indices, uint64_t index_count, const CfLightData* lights, uint32_t light_count,
+                       float* out, int threads)
+{
+    if (!ubo || !cam || !pc || !gbuf || !cells || !out) return 1;
+    const CfClusterForwardUBO& u = *ubo;
+    const uint32_t X = u.sliceCountX, Y = u.sliceCountY, Z = u.sliceCountZ;
+    const float pi = 3.14159265358979323846f;
+    if (threads <= 0) threads = omp_get_max_threads();
+    const int64_t n = int64_t(width) * height;
+    auto dot3 = [](const float a[3], const float b[3]) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; };
+    auto normalize3 = [&](const float v[3], float r[3]) {
+        const float l = cf_fsqrt(dot3(v, v));
+        for (int c = 0; c < 3; ++c) r[c] = v[c] / l;
+    };
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 256)
+    for (int64_t pix = 0; pix < n; ++pix) {
+        const CfGBufferTexel& t = gbuf[pix];
+        const float P[3] = {t.position[0], t.position[1], t.position[2]};
+        const float N[3] = {t.normal[0], t.normal[1], t.normal[2]};
+        const float A[3] = {t.albedo[0], t.albedo[1], t.albedo[2]};
+        const float metallic = t.normal[3], roughness = t.albedo[3];
+        const float cp[3] = {cam[0] - P[0], cam[1] - P[1], cam[2] - P[2]};
+        float V[3];
+        normalize3(cp, V);
+        const float NoV = gmax(dot3(N, V), 0.0f);
+        float F0[3], lo[3];
+        for (int c = 0; c < 3; ++c) {
+            F0[c] = pc->baseReflectivity * (1.0f - metallic) + A[c] * metallic;  // mix(x, y, a)
+            lo[c] = A[c] * pc->albedoMultipler;
+        }
+        const float alpha_r = ((roughness + 1.0f) * (roughness + 1.0f)) / 8.0f;
+        float alpha = 0.0f;
+        // the cluster lookup
+        const float near_ = u.cameraNear, far_ = u.cameraFar, zd = t.position[3];
+        const float lin = near_ * far_ / (far_ + zd * (near_ - far_));
+        const float zi = gmax(cf_log2_pinned(lin) * u.sliceScaling + u.sliceBias, 0.0f);
+        const float x = float(uint32_t(pix % width)) + 0.5f, y = float(uint32_t(pix / width)) + 0.5f;
+        const float xi = x / (u.screenSize[0] / float(X)), yi = y / (u.screenSize[1] / float(Y));
+        if (zi < float(Z) && xi < float(X) && yi < float(Y)) {
+            const CfLightCell cell = cells[uint32_t(xi) + uint32_t(yi) * X + uint32_t(zi) * X * Y];
+            if (uint64_t(cell.offset) + cell.count <= index_count) {
+                alpha = 1.0f;
+                for (uint32_t j = 0; j < cell.count; ++j) {
+                    const uint32_t li = indices[cell.offset + j];
+                    if (li >= light_count) {
+                        alpha = 0.0f;
+                        continue;
+                    }
+                    const CfLightData& L = lights[li];
+                    const float d[3] = {L.position[0] - P[0], L.position[1] - P[1], L.position[2] - P[2]};
+                    float Lv[3], h0[3], H[3];
+                    normalize3(d, Lv);
+                    for (int c = 0; c < 3; ++c) h0[c] = V[c] + Lv[c];
+                    normalize3(h0, H);
+                    const float NoH = gmax(dot3(N, H), 0.0f);
+                    const float NoL = gmax(dot3(N, Lv), 0.0f);
+                    const float HoV = gmax(dot3(H, V), 0.0f);
+                    const float dist = cf_fsqrt(dot3(d, d));
+                    const float att = gmax(1.0f - dist / L.radius, 0.0f) / cf_pow_pinned(dist, pc->lightFalloff);
+                    const float a = roughness * roughness, a2 = a * a;
+                    float den = (NoH * NoH) * (a2 - 1.0f) + 1.0f;
+                    den = pi * den * den;
+                    const float D = a2 / den;
+                    const float G = (NoL / (NoL * (1.0f - alpha_r) + alpha_r)) * (NoV / (NoV * (1.0f - alpha_r) + alpha_r));
+                    const float p5 = cf_pow_pinned(gmin(gmax(1.0f - HoV, 0.0f), 1.0f), 5.0f);
+                    const float denom = 4.0f * NoV * NoL + 0.0001f;
+                    for (int c = 0; c < 3; ++c) {
+                        const float F = F0[c] + (1.0f - F0[c]) * p5;
+                        const float spec = D * G * F / denom;
+                        const float kd = (1.0f - F) * (1.0f - metallic);
+                        const float diff = kd * A[c] / pi;
+                        const float rad = L.color[c] * att * pc->lightIntensity;
+                        lo[c] = lo[c] + (diff + spec) * rad * NoL;
+                    }
+                }
+            }
+        }
+        out[4 * pix + 0] = lo[0];
+        out[4 * pix + 1] = lo[1];
+        out[4 * pix + 2] = lo[2];
+        out[4 * pix + 3] = alpha;
+    }
+    return 0;
+}
+
+/*
+ * FrustumCulling.comp:14-57 for n boxes: instance[i] = 1 when box i may meet
+ * the frustum, else 0; dot(plane, (x, y, z, 1)) summed x, y, z, w in order.
+ */
+int cfo_frustum_cull(const CfFrustum* f, const CfAABB* boxes, uint32_t n, uint32_t* instance, int threads)
+{
+    if (!f || (n && (!boxes || !instance))) return 1;
+    if (threads <= 0) threads = omp_get_max_threads();
+    auto pd = [](const float* p, float x, float y, float z) { return ((p[0] * x + p[1] * y) + p[2] * z) + p[3] * 1.0f; };
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int64_t i = 0; i < int64_t(n); ++i) {
+        const CfAABB& b = boxes[i];
+        const float* mn = b.minPoint;
+        const float* mx = b.maxPoint;
+        bool in = true;
+        for (int k = 0; k < 6 && in; ++k) {
+            const float* p = f->planes[k];
+            int r = 0;
+            r += pd(p, mn[0], mn[1], mn[2]) < 0.0f;
+            r += pd(p, mx[0], mn[1], mn[2]) < 0.0f;
+            r += pd(p, mn[0], mx[1], mn[2]) < 0.0f;
+            r += pd(p, mx[0], mx[1], mn[2]) < 0.0f;
+            r += pd(p, mn[0], mn[1], mx[2]) < 0.0f;
+            r += pd(p, mx[0], mn[1], mx[2]) < 0.0f;
+            r += pd(p, mn[0], mx[1], mx[2]) < 0.0f;
+            r += pd(p, mx[0], mx[1], mx[2]) < 0.0f;
+            if (r == 8) in = false;
+        }
+        for (int a = 0; a < 3 && in; ++a) {
+            int above = 0, below = 0;
+            for (int c = 0; c < 8; ++c) {
+                above += f->corners[c][a] > mx[a];
+                below += f->corners[c][a] < mn[a];
+            }
+            if (above == 8 || below == 8) in = false;
+        }
+        instance[i] = in ? 1u : 0u;
     }
     return 0;
 }

@@ -189,3 +189,19 @@ def test_oracle_lookup_flags_cells_that_leave_the_index_list(oracle):
     s = oracle.lookup_clusters(v.ubo, depth, cells, wrong, v.lights, 150, a)
     listed = good["count"] > 0
     assert np.all((s["flags"][listed] & FRAGMENT_BAD_CELL) > 0) and np.all(s["covering"] == 0)
+
+
+def test_oracle_frustum_culling_keeps_what_the_camera_sees():
+    """Boxes around points in front of the camera are kept, boxes behind it or
+    beyond the far plane are not (oracle only)."""
+    from hellovulkan_gb300.camera import frustum_ubo, look_at_rh
+    from oracle import Oracle
+    o = Oracle()
+    f = frustum_ubo(math.radians(60.0), 1.0, 0.1, 100.0, look_at_rh((0.0, 0.0, 0.0), (0.0, 0.0, -1.0)))
+    def box(c, h=0.5):
+        b = np.zeros(8, np.float32)
+        b[0:3] = np.array(c) - h
+        b[4:7] = np.array(c) + h
+        return b
+    boxes = np.stack([box((0, 0, -10)), box((0, 0, 10)), box((0, 0, -200)), box((50, 0, -10)), box((0, 0, -99.9))])
+    assert o.frustum_cull(f, boxes).tolist() == [1, 0, 0, 0, 1]

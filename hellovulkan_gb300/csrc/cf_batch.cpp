@@ -37,8 +37,8 @@ using namespace cfrt;
 namespace {
 
 const cfk::CullConfig kBatchCandidates[] = {
-    {1, 4, 128, 4, 1}, {2, 4, 128, 4, 1}, {4, 4, 128, 4, 1}, {1, 8, 128, 4, 1}, {2, 8, 128, 4, 1}, {4, 8, 128, 4, 1},
     {1, 4, 256, 4, 1}, {2, 4, 256, 4, 1}, {4, 4, 256, 4, 1}, {1, 8, 256, 4, 1}, {2, 8, 256, 4, 1}, {4, 8, 256, 4, 1},
+    {2, 4, 512, 2, 1}, {4, 4, 512, 2, 1}, {2, 8, 512, 2, 1}, {4, 8, 512, 2, 1}, {2, 8, 1024, 2, 1}, {4, 8, 1024, 2, 1},
 };
 const cfk::CullConfig kBatchDefault = {2, 8, 256, 4, 1};
 

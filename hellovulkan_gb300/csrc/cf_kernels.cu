@@ -1271,12 +1271,12 @@ cudaError_t launch_cull_t(const ViewCull& v, uint32_t* dev_error, cudaStream_t s
     X(1, 8, 256, 4, true)   \
     X(2, 8, 256, 4, true)   \
     X(4, 8, 256, 4, true)   \
-    X(1, 4, 128, 4, true)   \
-    X(2, 4, 128, 4, true)   \
-    X(4, 4, 128, 4, true)   \
-    X(1, 8, 128, 4, true)   \
-    X(2, 8, 128, 4, true)   \
-    X(4, 8, 128, 4, true)
+    X(2, 4, 512, 2, true)   \
+    X(4, 4, 512, 2, true)   \
+    X(2, 8, 512, 2, true)   \
+    X(4, 8, 512, 2, true)   \
+    X(2, 8, 1024, 2, true)  \
+    X(4, 8, 1024, 2, true)
 
 bool cull_config_supported(const CullConfig& c)
 {

@@ -99,7 +99,7 @@ def test_batch_autotune_and_every_configuration_stay_exact(gpu, oracle):
     s = torch.cuda.Stream()
     b.generate_aabbs(s)
     keys = sorted({v.grid[0] * v.grid[1] for v in views})
-    for cfg in [(1, 4, 128, 4), (4, 8, 128, 4), (2, 4, 256, 4), (4, 8, 256, 4)]:
+    for cfg in [(1, 4, 256, 4), (4, 8, 256, 4), (2, 4, 512, 2), (4, 8, 1024, 2)]:
         for k in keys:
             b.set_tuning(k, *cfg)
         b.cull(s)

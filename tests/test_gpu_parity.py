@@ -10,7 +10,8 @@ from hellovulkan_gb300.camera import look_at_rh, ubo_from_bytes
 
 pytestmark = pytest.mark.gpu
 
-TUNINGS = [(k, w, 512, 4, 0) for k in (1, 2, 4) for w in (4, 8)] + [(k, w, 256, 4, 1) for k in (1, 2, 4) for w in (4, 8)]
+TUNINGS = ([(k, w, 512, 4, 0) for k in (1, 2, 4) for w in (4, 8)] + [(k, w, 256, 4, 1) for k in (1, 2, 4) for w in (4, 8)]
+           + [(k, w, 512, 2, 1) for k in (2, 4) for w in (4, 8)] + [(k, 8, 1024, 2, 1) for k in (2, 4)])
 
 
 def golden_views(golden):

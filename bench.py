@@ -602,11 +602,13 @@ def run_ours(args):
 
     cull.set_cluster_forward_ubo(view.ubo)
     cull_cfg_used = cull.tuning()
-    cull.enable_stage_timing(True)
 
-    def timed_steps(n):
+    def timed_steps(n, stages=False):
         """n steps, L2 flushed before each, each bracketed by CUDA events on the
-        launching stream; returns (sum of step ms, per-step stage ms)."""
+        launching stream; returns (sum of step ms, per-step stage ms).  With
+        stages, the pipeline also records its per-stage events (which add a
+        little device time) and each step is read back before the next."""
+        cull.enable_stage_timing(stages)
         starts = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
         ends = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
         stage = np.zeros((n, 3))
@@ -616,8 +618,10 @@ def run_ours(args):
             starts[i].record(stream)
             cull.fill_command_buffer(stream)
             ends[i].record(stream)
-            stage[i] = cull.stage_times_ms()
+            if stages:
+                stage[i] = cull.stage_times_ms()
         torch.cuda.synchronize()
+        cull.enable_stage_timing(False)
         return float(sum(s.elapsed_time(e) for s, e in zip(starts, ends))), stage
 
     for _ in range(args.warmup):
@@ -628,7 +632,8 @@ def run_ours(args):
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    total_ms, stage = timed_steps(args.steps)
+    total_ms, _ = timed_steps(args.steps)
+    _, stage = timed_steps(max(3, min(args.steps, 100)), stages=True)  # the per-stage breakdown, untimed
 
     # e2e through the C ABI with host buffers
     b = rc.buffers()
@@ -662,14 +667,13 @@ def run_ours(args):
     cull.fill_command_buffer(stream)
     work_filter, work_cluster = cull.read_work_counters()
     cull.enable_work_counters(False)
-    cull.enable_stage_timing(True)
     plain_steps = max(3, min(args.steps, 200))
     cull.set_tuning(*(PLAIN_SMALL if view.clusters <= 8192 else PLAIN_LARGE))
     for _ in range(3):
         cull.fill_command_buffer(stream)
-    plain_ms, plain_stage = timed_steps(plain_steps)
+    plain_ms, _ = timed_steps(plain_steps)
+    _, plain_stage = timed_steps(max(3, min(plain_steps, 50)), stages=True)
     cull.set_tuning(0)
-    cull.enable_stage_timing(False)
 
     batched = None
     if not args.no_batch and rank == 0:

@@ -40,7 +40,7 @@ const cfk::CullConfig kBatchCandidates[] = {
     {1, 4, 256, 4, 1}, {2, 4, 256, 4, 1}, {4, 4, 256, 4, 1}, {1, 8, 256, 4, 1}, {2, 8, 256, 4, 1}, {4, 8, 256, 4, 1},
     {2, 4, 512, 2, 1}, {4, 4, 512, 2, 1}, {2, 8, 512, 2, 1}, {4, 8, 512, 2, 1}, {2, 8, 1024, 2, 1}, {4, 8, 1024, 2, 1},
 };
-const cfk::CullConfig kBatchDefault = {2, 8, 256, 4, 1};
+const cfk::CullConfig kBatchDefault = {2, 8, 1024, 2, 1};
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 

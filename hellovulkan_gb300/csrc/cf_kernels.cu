@@ -1179,35 +1179,56 @@ __device__ __forceinline__ void copy_body(const ViewCull& v, uint32_t blk)
     }
 }
 
-// One warp per cluster (a single view has too few groups to fill the GPU
-// with one warp each): the cluster's offset is its group's offset plus the
-// counts of the group's earlier clusters.
-__device__ __forceinline__ void copy_cluster_body(const ViewCull& v, uint32_t blk)
+// A single view: one 256-thread CTA per cluster group (a view has too few
+// groups to fill the GPU with one warp each, and a group of capped clusters
+// holds thousands of hits).  Warp 0 writes the group's cells from its counts
+// (a warp scan on top of the group's offset); then all threads move the hits
+// from the staging rows to the packed list, each finding its cluster by a
+// binary search over the exclusive sums, four loads in flight per thread.
+constexpr uint32_t kCopyThreads = 256, kCopyBlockIlp = 4;
+__global__ void __launch_bounds__(kCopyThreads) copy_kernel(const ViewCull v)
 {
-    const uint32_t c = blk * kCopyWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (c >= v.clusters) return;
-    uint32_t b, first;
-    if (v.binned) {
-        const uint32_t gps = (v.slice_clusters + v.group_width - 1) / v.group_width;
-        const uint32_t k = c / v.slice_clusters, gi = (c % v.slice_clusters) / v.group_width;
-        b = k * gps + gi;
-        first = k * v.slice_clusters + gi * v.group_width;
-    } else {
-        b = c / v.group_width;
-        first = b * v.group_width;
+    __shared__ uint32_t s_excl[33];
+    __shared__ uint32_t s_base;
+    const uint32_t b = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
+    uint32_t first, end;
+    group_range(v, b, &first, &end);
+    if (tid < 32) {
+        const uint32_t c = first + lane;
+        const uint32_t cnt = c < end ? v.counts[c] : 0u;
+        const uint32_t incl = warp_inclusive_scan(cnt, lane);
+        const uint32_t base = v.group_offsets[b];
+        if (c < end) v.cells[c] = CfLightCell{base + incl - cnt, cnt};
+        s_excl[lane] = incl - cnt;  // lanes past the group hold the group's total
+        if (lane == 31) {
+            s_excl[32] = incl;
+            s_base = base;
+        }
     }
-    const uint32_t cj = first + lane;
-    const uint32_t before = warp_sum(cj < c ? v.counts[cj] : 0u);
-    const uint32_t n = v.counts[c];
-    const uint32_t offset = v.group_offsets[b] + before;
-    if (lane == 0) v.cells[c] = CfLightCell{offset, n};
-    const uint32_t* src = v.staging + (size_t)c * v.cap;
-    for (uint32_t i = lane; i < n; i += 32) v.indices[offset + i] = src[i];
-}
-
-__global__ void __launch_bounds__(kCopyWarps * 32) copy_kernel(const ViewCull v)
-{
-    copy_cluster_body(v, blockIdx.x);
+    __syncthreads();
+    const uint32_t total = s_excl[32], base = s_base;
+    const uint32_t* __restrict__ staging = v.staging;
+    uint32_t* __restrict__ indices = v.indices;
+    for (uint32_t i0 = 0; i0 < total; i0 += kCopyThreads * kCopyBlockIlp) {
+        uint32_t val[kCopyBlockIlp];
+#pragma unroll
+        for (uint32_t u = 0; u < kCopyBlockIlp; ++u) {
+            const uint32_t i = i0 + u * kCopyThreads + tid;
+            val[u] = 0;
+            if (i < total) {
+                uint32_t q = 0;  // the last cluster whose exclusive sum is <= i
+#pragma unroll
+                for (uint32_t step = 16; step; step >>= 1)
+                    if (s_excl[q + step] <= i) q += step;
+                val[u] = __ldg(&staging[(size_t)(first + q) * v.cap + (i - s_excl[q])]);
+            }
+        }
+#pragma unroll
+        for (uint32_t u = 0; u < kCopyBlockIlp; ++u) {
+            const uint32_t i = i0 + u * kCopyThreads + tid;
+            if (i < total) indices[base + i] = val[u];
+        }
+    }
 }
 
 // Batched copy: block b is copy block b - prefix[v] of view v.
@@ -1295,7 +1316,7 @@ constexpr uint64_t kBinnedMinTests = 16ull << 20;
 
 CullConfig default_cull_config(uint32_t clusters, uint32_t lights, uint32_t slices)
 {
-    if (slices >= 2 && (uint64_t)clusters * lights >= kBinnedMinTests) return CullConfig{2, 8, 256, 4, 1};
+    if (slices >= 2 && (uint64_t)clusters * lights >= kBinnedMinTests) return CullConfig{2, 8, 1024, 2, 1};
     if (clusters <= 8192) return CullConfig{1, 8, 512, 4, 0};
     return CullConfig{2, 8, 512, 4, 0};
 }
@@ -1379,7 +1400,7 @@ cudaError_t launch_finalize(const ViewCull& v, cudaStream_t stream)
     scan_kernel<<<1, kScanThreads, 0, stream>>>(v);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    copy_kernel<<<(v.clusters + kCopyWarps - 1) / kCopyWarps, kCopyWarps * 32, 0, stream>>>(v);
+    copy_kernel<<<v.groups, kCopyThreads, 0, stream>>>(v);
     return cudaGetLastError();
 }
 

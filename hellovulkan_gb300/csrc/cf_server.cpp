@@ -199,7 +199,10 @@ cfk::CullConfig server_config_for(const CfServer* s, uint32_t xy)
 {
     auto it = s->tuned.find(xy);
     if (it != s->tuned.end()) return it->second;
-    return xy <= 64 ? cfk::CullConfig{2, 4, 256, 4, 1} : cfk::CullConfig{4, 4, 256, 4, 1};
+    // what the batch autotuner picks for the served mix's four grids on a GB300
+    if (xy <= 64) return cfk::CullConfig{2, 4, 512, 2, 1};
+    if (xy <= 144) return cfk::CullConfig{4, 4, 512, 2, 1};
+    return cfk::CullConfig{4, 8, 1024, 2, 1};
 }
 
 void free_version_if_dead(CfServer* s, LightVersion* v)

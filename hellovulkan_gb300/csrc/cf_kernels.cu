@@ -618,7 +618,7 @@ struct PipeSmem {
 };
 
 template <int K, int WARPS, int TILE, int STAGES>
-__global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 4 : 2)
+__global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
     cull_pipe_kernel(const ViewJob* __restrict__ jobs, const uint2* __restrict__ items, uint32_t n_items,
                      uint32_t* __restrict__ queue, uint32_t* __restrict__ dev_error, const ViewCull single)
 {
@@ -769,7 +769,7 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 4 : 2)
         }
         consumer_sync<WARPS * 32>();  // every warp leaves together on a timeout
         if (*s_abort) break;
-        const ItemDesc d = desc[r];
+        const ItemDesc& d = desc[r];  // read in place: the slot is not refilled before this item's release
         if (d.flags & kItemTerminate) break;
         const uint32_t cl0 = d.first + warp * (uint32_t)K;
         const float4* gb = boxes + (size_t)r * kGroup * 2 + (size_t)warp * K * 2;

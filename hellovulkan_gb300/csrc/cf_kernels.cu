@@ -1528,8 +1528,15 @@ cudaError_t batch_occupancy_t(int* blocks)
         *blocks = 0;
         return cudaErrorInvalidValue;
     } else {
+        // the opt-in above 48 KB must precede the query, or it reports 0 blocks
+        const size_t smem = PipeSmem<K, WARPS, TILE, STAGES>::bytes;
+        if (smem > 48 * 1024) {
+            const cudaError_t e = cudaFuncSetAttribute(cull_pipe_kernel<K, WARPS, TILE, STAGES>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, cull_pipe_kernel<K, WARPS, TILE, STAGES>,
-                                                             (WARPS + 1) * 32, PipeSmem<K, WARPS, TILE, STAGES>::bytes);
+                                                             (WARPS + 1) * 32, smem);
     }
 }
 

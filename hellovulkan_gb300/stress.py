@@ -144,6 +144,9 @@ class StressAnimation:
         self.frame_index = 0
         for f in range(frames):
             if f % self.frames_per_projection == 0:
+                # the re-plan waits for the frames already queued; drain them first so
+                # that the time below is the host's own planning work
+                stream.synchronize()
                 t0 = time.perf_counter()
                 self.plan_epoch(f // self.frames_per_projection)
                 plan_ms.append(1e3 * (time.perf_counter() - t0))

@@ -63,6 +63,26 @@ def test_batch_matches_oracle_with_graph_replays(gpu, oracle):
     assert info["views"] == len(views) and info["buckets"] >= 2
 
 
+def test_batch_persistent_grid_counts_large_shared_memory_configs(gpu):
+    """A configuration above 48 KB of shared memory must size its persistent
+    grid from the real occupancy before its first launch, not from one CTA per SM."""
+    import torch
+    from hellovulkan_gb300.batch import Batch, BatchBuffers
+    views = scenes.batch_mix(3, 64)  # enough work items that no bucket is capped by its item count
+    bufs = BatchBuffers(views)
+    b = Batch(gpu)
+    keys = sorted({v.grid[0] * v.grid[1] for v in views})
+    for xy in keys:
+        b.set_tuning(xy, 4, 8, 1024, 2)  # 8 warps, 1024-light stages x2: > 48 KB
+    b.set_views(bufs.batch_views())
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    buckets = b.info()["bucket_configs"]
+    assert all(bc["config"] == [4, 8, 1024, 2] for bc in buckets)
+    assert max(bc["ctas"] for bc in buckets) >= 2 * sms, buckets
+    b.close()
+    del bufs
+
+
 def test_batch_without_graph_and_new_view_matrices(gpu, oracle):
     import torch
     from hellovulkan_gb300.batch import Batch, BatchBuffers

@@ -62,6 +62,16 @@ def test_every_kernel_configuration(gpu, oracle, golden, tuning):
     assert_matches_oracle(oracle, v, *run_pipeline(gpu, v, tuning))
 
 
+@pytest.mark.parametrize("tuning", [(2, 8, 1024, 2, 1), (4, 8, 1024, 2, 1), (4, 4, 512, 2, 1), (2, 8, 256, 4, 1)])
+def test_dense_slices_with_a_short_last_group(gpu, oracle, tuning):
+    """Slices with thousands of candidates (several tiles per cluster group)
+    on a 15-wide grid, whose last group per slice is short."""
+    rng = np.random.default_rng(17)
+    lights = scenes.uniform_box_lights(rng, 8000, [-30, -15, -60], [30, 15, -5], 2.0, 6.0)
+    v = scenes.custom_view((15, 9, 24), 1920, 1080, 0.1, 300.0, lights=lights)
+    assert_matches_oracle(oracle, v, *run_pipeline(gpu, v, tuning))
+
+
 def test_batch_mix_views(gpu, oracle):
     views = scenes.batch_mix(3, n_views=12)
     views.sort(key=lambda v: -v.light_count)

@@ -791,7 +791,8 @@ def run_ours(args):
         "e2e": {"value": ws * tests_per_view * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": bi,
                 "d2h_bytes_per_step": bo, "ms_per_step": 1e3 * e2e_s / e2e_steps, "steps": e2e_steps,
                 "timing": "host clock, synchronised, pinned host buffers"},
-        "gpu_launches": 4 * (args.steps + e2e_steps),
+        # our kernels per step: light transform, [slice binning,] culling, offset scan, copy
+        "gpu_launches": (5 if cull_cfg_used[4] else 4) * (args.steps + e2e_steps),
         "clocks": clocks,
         "batched": batched,
         "served": served,

@@ -1405,6 +1405,57 @@ cudaError_t launch_finalize(const ViewCull& v, cudaStream_t stream)
 }
 
 // ---------------------------------------------------------------------------
+// Read-back into host memory the device can address (pinned and mapped, on
+// this system over NVLink-C2C): the hit total, the LightCells and the first
+// min(total, capacity) indices, in one launch with no host round trip for the
+// count.  Grid-stride over 32-bit words, 16 bytes per access where both sides
+// are 16-byte aligned.
+// ---------------------------------------------------------------------------
+namespace {
+
+__device__ __forceinline__ void copy_words(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, uint64_t n,
+                                           bool vec, uint64_t tid, uint64_t stride)
+{
+    uint64_t head = 0;
+    if (vec) {
+        const uint64_t n4 = n / 4;
+        const uint4* s4 = reinterpret_cast<const uint4*>(src);
+        uint4* d4 = reinterpret_cast<uint4*>(dst);
+        for (uint64_t i = tid; i < n4; i += stride) d4[i] = s4[i];
+        head = n4 * 4;
+    }
+    for (uint64_t i = head + tid; i < n; i += stride) dst[i] = src[i];
+}
+
+__global__ void __launch_bounds__(256) readback_kernel(const uint32_t* __restrict__ cells, uint32_t cell_words,
+                                                       const uint32_t* __restrict__ indices,
+                                                       const uint32_t* __restrict__ d_total, uint64_t capacity,
+                                                       uint32_t* __restrict__ h_cells, uint32_t* __restrict__ h_indices,
+                                                       uint32_t* __restrict__ h_total, bool vec_cells, bool vec_indices)
+{
+    const uint32_t total = *d_total;
+    const uint64_t tid = (uint64_t)blockIdx.x * 256 + threadIdx.x, stride = (uint64_t)gridDim.x * 256;
+    if (tid == 0) *h_total = total;
+    if (h_cells) copy_words(cells, h_cells, cell_words, vec_cells, tid, stride);
+    if (h_indices) copy_words(indices, h_indices, total < capacity ? total : capacity, vec_indices, tid, stride);
+}
+
+}  // namespace
+
+cudaError_t launch_readback(const CfLightCell* cells, uint32_t clusters, const uint32_t* indices,
+                            const uint32_t* d_total, uint64_t capacity, CfLightCell* h_cells, uint32_t* h_indices,
+                            uint32_t* h_total, cudaStream_t stream)
+{
+    auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+    const uint64_t words = std::max<uint64_t>(2ull * clusters, h_indices ? capacity : 0ull);
+    const uint32_t blocks = (uint32_t)std::min<uint64_t>(std::max<uint64_t>((words + 1023) / 1024, 1ull), 1216ull);
+    readback_kernel<<<blocks, 256, 0, stream>>>(reinterpret_cast<const uint32_t*>(cells), 2u * clusters, indices,
+                                                d_total, capacity, reinterpret_cast<uint32_t*>(h_cells), h_indices,
+                                                h_total, al16(cells) && al16(h_cells), al16(indices) && al16(h_indices));
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Light jitter: dst = src with every position coordinate moved by sigma times
 // an Irwin-Hall variate (the sum of 12 uniforms in [0, 1) minus 6, mean 0,
 // variance 1, a close stand-in for a unit Gaussian).  The uniforms come from

@@ -130,6 +130,10 @@ cudaError_t launch_light_xform(const CfLightData* lights, uint32_t count, const 
 cudaError_t launch_bin(const ViewCull& v, cudaStream_t stream);
 cudaError_t launch_cull(const ViewCull& v, const CullConfig& cfg, uint32_t* dev_error, cudaStream_t stream);
 cudaError_t launch_finalize(const ViewCull& v, cudaStream_t stream);
+// total, cells and min(total, capacity) indices of one view into device-addressable host memory
+cudaError_t launch_readback(const CfLightCell* cells, uint32_t clusters, const uint32_t* indices,
+                            const uint32_t* d_total, uint64_t capacity, CfLightCell* h_cells, uint32_t* h_indices,
+                            uint32_t* h_total, cudaStream_t stream);
 // dst = src with positions moved by sigma * (Irwin-Hall variate) from (seed, light, axis).
 cudaError_t launch_jitter(const CfLightData* src, CfLightData* dst, uint32_t n, uint64_t seed, float sigma,
                           cudaStream_t stream);

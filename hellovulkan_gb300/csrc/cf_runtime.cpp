@@ -47,6 +47,21 @@ int cuda_fail(cudaError_t e, const char* what)
     return fail(CF_ERROR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
+// True for host memory the current device can address (pinned and mapped);
+// *dev receives the device-side address.  Other pointers (pageable, device)
+// return false and leave no CUDA error behind.
+bool device_addressable(const void* host, void** dev)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return false;
+    *dev = a.devicePointer;
+    return true;
+}
+
 bool projection_equal(const CfClusterForwardUBO& a, const CfClusterForwardUBO& b)
 {
     return memcmp(a.cameraInverseProjection, b.cameraInverseProjection, sizeof(a.cameraInverseProjection)) == 0 &&
@@ -200,6 +215,7 @@ struct CfResourcesClusterForward {
     uint32_t* d_total = nullptr;
     unsigned char* d_ws = nullptr;
     size_t ws_capacity = 0;
+    uint32_t* h_total = nullptr;  // pinned word the one-launch read-back writes the total into
     bool aabb_dirty = true;
     bool aabb_built = false;
     CfClusterForwardUBO built_from{};
@@ -409,6 +425,7 @@ int cf_resources_cluster_forward_destroy(CfResourcesClusterForward* r)
     if (!r) return CF_SUCCESS;
     DeviceGuard g(r->ctx->device);
     free_cluster_buffers(r);
+    if (r->h_total) cudaFreeHost(r->h_total);
     delete r;
     return CF_SUCCESS;
 }
@@ -473,6 +490,26 @@ int cf_resources_cluster_forward_read_outputs(CfResourcesClusterForward* r, CfLi
     if (!r->d_cells) return fail(CF_ERROR_NOT_READY, "buffers were never created");
     DeviceGuard g(r->ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
+    // Host buffers the device can address (pinned, mapped): one read-back
+    // launch writes the total, the cells and the indices, then one wait.
+    void* dev_cells = nullptr;
+    void* dev_indices = nullptr;
+    if ((!host_cells || device_addressable(host_cells, &dev_cells)) &&
+        (!host_indices || device_addressable(host_indices, &dev_indices)) &&
+        (r->h_total || cudaHostAlloc(reinterpret_cast<void**>(&r->h_total), sizeof(uint32_t), cudaHostAllocMapped) ==
+                           cudaSuccess)) {
+        void* dev_total = nullptr;
+        cudaError_t e = cudaHostGetDevicePointer(&dev_total, r->h_total, 0);
+        if (e == cudaSuccess)
+            e = cfk::launch_readback(r->d_cells, r->clusters, r->d_indices, r->d_total, host_indices ? host_index_capacity : 0,
+                                     static_cast<CfLightCell*>(dev_cells), static_cast<uint32_t*>(dev_indices),
+                                     static_cast<uint32_t*>(dev_total), st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return cuda_fail(e, "read outputs");
+        *total = *reinterpret_cast<volatile uint32_t*>(r->h_total);
+        return CF_SUCCESS;
+    }
+    cudaGetLastError();  // a failed pinned-word allocation leaves no sticky error
     uint32_t t = 0;
     cudaError_t e = cudaMemcpyAsync(&t, r->d_total, sizeof(t), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess && host_cells)

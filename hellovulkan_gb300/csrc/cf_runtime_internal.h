@@ -18,6 +18,7 @@ int fail(int status, const char* fmt, ...) __attribute__((format(printf, 2, 3)))
 int cuda_fail(cudaError_t e, const char* what);
 
 bool projection_equal(const CfClusterForwardUBO& a, const CfClusterForwardUBO& b);
+bool device_addressable(const void* host, void** dev);
 int validate_grid(uint32_t x, uint32_t y, uint32_t z, uint32_t cap, uint32_t* clusters);
 
 // Makes `device` current for the guard's lifetime.

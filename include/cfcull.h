@@ -130,7 +130,11 @@ CFCULL_API int cf_resources_cluster_forward_get_buffers(const CfResourcesCluster
 /* ResourcesClusterForward::aabbDirty_ */
 CFCULL_API int cf_resources_cluster_forward_is_aabb_dirty(const CfResourcesClusterForward* res, int* dirty);
 /* Copies the cells and the first min(total, host_index_capacity) indices to
- * host memory and returns the total; synchronises `stream`. */
+ * host memory and returns the total; synchronises `stream`.  When both host
+ * buffers are pinned memory the device can address (cudaHostAlloc /
+ * cudaHostRegister, e.g. torch's pin_memory), one kernel writes total, cells
+ * and indices straight into them and the call waits once; other buffers go
+ * through two copies and two waits (the total first, then the indices). */
 CFCULL_API int cf_resources_cluster_forward_read_outputs(CfResourcesClusterForward* res, CfLightCell* host_cells,
                                                          uint32_t* host_indices, uint64_t host_index_capacity,
                                                          uint32_t* total, void* stream);

@@ -72,6 +72,43 @@ def test_dense_slices_with_a_short_last_group(gpu, oracle, tuning):
     assert_matches_oracle(oracle, v, *run_pipeline(gpu, v, tuning))
 
 
+def test_read_outputs_into_pinned_memory(gpu, oracle):
+    """The one-launch read-back into pinned host buffers gives what the
+    two-copy path gives: the full lists, and a prefix for a short index buffer."""
+    import torch
+    from hellovulkan_gb300.pipelines import (PipelineAABBGenerator, PipelineLightCulling, ResourcesClusterForward,
+                                             ResourcesLight)
+    v = scenes.plain_large(4, n_lights=8000)
+    rl = ResourcesLight(gpu)
+    rl.add_lights(v.lights)
+    rc = ResourcesClusterForward(gpu)
+    rc.create_buffers(*v.grid, v.cap)
+    gen = PipelineAABBGenerator(gpu, rc)
+    gen.set_cluster_forward_ubo(v.ubo)
+    gen.fill_command_buffer()
+    cull = PipelineLightCulling(gpu, rl, rc)
+    cull.set_cluster_forward_ubo(v.ubo)
+    cull.fill_command_buffer()
+    cells_p, idx_p = rc.read_outputs()  # pageable numpy buffers: two copies
+    oc, oi, _ = oracle.cull(v.ubo, oracle.generate_aabbs(v.ubo), v.lights, v.cap)
+    assert np.array_equal(cells_p, oc) and np.array_equal(idx_p, oi)
+    b = rc.buffers()
+    pinned = [torch.zeros((b.cluster_count, 2), dtype=torch.int32).pin_memory(),
+              torch.zeros(b.index_capacity, dtype=torch.int32).pin_memory(),
+              torch.zeros(1001, dtype=torch.int32).pin_memory()]
+    h_cells, h_idx, h_short = (t.numpy().view(np.uint32) for t in pinned)
+    s = torch.cuda.Stream()
+    cells, idx = rc.read_outputs(s, h_cells, h_idx)
+    assert np.array_equal(cells, oc) and np.array_equal(idx, oi)
+    # a short host index buffer (offset by one word: no 16-byte accesses) gets a prefix
+    short = h_short[1:]
+    _, part = rc.read_outputs(s, h_cells, short)
+    assert part.size == min(oi.size, short.size) and np.array_equal(part, oi[:part.size])
+    assert gpu.check_device_error() == 0
+    for o in (cull, gen, rc, rl):
+        o.close()
+
+
 def test_batch_mix_views(gpu, oracle):
     views = scenes.batch_mix(3, n_views=12)
     views.sort(key=lambda v: -v.light_count)

@@ -29,6 +29,7 @@
 #include "cf_kernels.cuh"
 
 #include <algorithm>
+#include <utility>
 
 #include "cf_pinned_math.h"
 
@@ -120,6 +121,16 @@ __device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void* src, uin
         : "memory");
 }
 
+// Programmatic dependent launch.  The kernels of one view's step are launched
+// with programmatic stream serialisation, so each may be scheduled while the
+// previous kernel of the stream is still running: it runs only its prologue
+// (barrier init, parameters) before grid_dependency_wait(), which returns
+// once every earlier kernel of the stream has completed and its writes are
+// visible.  launch_dependents() lets the next kernel be scheduled early.
+// Both are no-ops in a launch without a programmatic dependency.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Named barrier 1 over the first N threads of the CTA (the consumer warps;
 // the producer warp never takes part).
 template <int N>
@@ -138,13 +149,6 @@ __device__ __forceinline__ float max3f(float a, float b, float c)
 __device__ __forceinline__ bool finite_bits(float x)
 {
     return (__float_as_uint(x) & 0x7f800000u) != 0x7f800000u;
-}
-
-__device__ __forceinline__ uint32_t warp_sum(uint32_t x)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
-    return x;
 }
 
 __device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t x, uint32_t lane)
@@ -253,6 +257,8 @@ __global__ void __launch_bounds__(kFlagGranule) light_xform_kernel(const CfLight
                                                                    float4* __restrict__ out,
                                                                    uint32_t* __restrict__ nonfinite)
 {
+    grid_dependency_wait();
+    launch_dependents();
     light_xform_body(lights, count, lpad, view.m, out, nonfinite, blockIdx.x);
 }
 
@@ -460,6 +466,8 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
     CullSmem<K, WARPS, TILE, STAGES> sm(smem);
     sm.init();
     __syncthreads();
+    grid_dependency_wait();
+    launch_dependents();
     const uint32_t group = blockIdx.x;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t nsrc = v.lpad, first = group * (uint32_t)(WARPS * K), cl_end = v.clusters;
@@ -666,6 +674,8 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
         mbar_init_fence();
     }
     __syncthreads();
+    grid_dependency_wait();  // a single view's launch may overlap the binning launch's tail
+    launch_dependents();
 
     if (warp == WARPS) {
         // Producer: lane 0 fetches items, fills descriptors, loads AABBs and
@@ -1056,6 +1066,8 @@ __device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
 
 __global__ void __launch_bounds__(kBinWarpsSingle * 32) bin_slices_kernel(const ViewCull v)
 {
+    grid_dependency_wait();
+    launch_dependents();
     bin_slices_body<kBinWarpsSingle, kBinSlicesSingle>(v, blockIdx.x);
 }
 
@@ -1128,6 +1140,8 @@ constexpr uint32_t kCopyWarps = 8;
 constexpr uint32_t kCopyIlp = 8;
 __global__ void __launch_bounds__(kScanThreads) scan_kernel(const ViewCull v)
 {
+    grid_dependency_wait();
+    launch_dependents();
     scan_body(v);
 }
 
@@ -1190,6 +1204,7 @@ __global__ void __launch_bounds__(kCopyThreads) copy_kernel(const ViewCull v)
 {
     __shared__ uint32_t s_excl[33];
     __shared__ uint32_t s_base;
+    grid_dependency_wait();
     const uint32_t b = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
     uint32_t first, end;
     group_range(v, b, &first, &end);
@@ -1240,6 +1255,26 @@ __global__ void __launch_bounds__(kCopyWarps * 32) batch_copy_kernel(const ViewJ
     copy_body(jobs[vi].v, blockIdx.x - __ldg(&prefix[vi]));
 }
 
+// Launches `kernel` with programmatic stream serialisation (see
+// grid_dependency_wait): it may be scheduled while the stream's previous
+// kernel is still running.
+template <typename... Params, typename... Args>
+cudaError_t launch_overlapped(void (*kernel)(Params...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                              Args&&... args)
+{
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 template <int K, int WARPS, int TILE, int STAGES, bool kBinned>
 cudaError_t launch_cull_t(const ViewCull& v, uint32_t* dev_error, cudaStream_t stream)
 {
@@ -1261,9 +1296,9 @@ cudaError_t launch_cull_t(const ViewCull& v, uint32_t* dev_error, cudaStream_t s
         }();
         if (resident <= 0) return cudaErrorInvalidConfiguration;
         const uint32_t ctas = std::min<uint32_t>(v.groups, (uint32_t)resident);
-        cull_pipe_kernel<K, WARPS, TILE, STAGES>
-            <<<ctas, (WARPS + 1) * 32, psmem, stream>>>(nullptr, nullptr, v.groups, v.queue, dev_error, v);
-        return cudaGetLastError();
+        return launch_overlapped(cull_pipe_kernel<K, WARPS, TILE, STAGES>, dim3(ctas), dim3((WARPS + 1) * 32), psmem,
+                                 stream, static_cast<const ViewJob*>(nullptr), static_cast<const uint2*>(nullptr),
+                                 v.groups, v.queue, dev_error, v);
     } else {
         const size_t smem = CullSmem<K, WARPS, TILE, STAGES>::bytes();
         if (smem > 48 * 1024) {  // opt in above the default 48 KB (a per-device attribute)
@@ -1271,8 +1306,8 @@ cudaError_t launch_cull_t(const ViewCull& v, uint32_t* dev_error, cudaStream_t s
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
         }
-        cull_kernel<K, WARPS, TILE, STAGES><<<v.groups, (WARPS + 1) * 32, smem, stream>>>(v, dev_error);
-        return cudaGetLastError();
+        return launch_overlapped(cull_kernel<K, WARPS, TILE, STAGES>, dim3(v.groups), dim3((WARPS + 1) * 32), smem,
+                                 stream, v, dev_error);
     }
 }
 
@@ -1369,15 +1404,15 @@ cudaError_t launch_light_xform(const CfLightData* lights, uint32_t count, const 
     if (lpad == 0) return cudaSuccess;
     Mat4 m;
     for (int i = 0; i < 16; ++i) m.m[i] = view[i];
-    light_xform_kernel<<<granules(lpad), kFlagGranule, 0, stream>>>(lights, count, lpad, m, vlights, nonfinite);
-    return cudaGetLastError();
+    return launch_overlapped(light_xform_kernel, dim3(granules(lpad)), dim3(kFlagGranule), 0, stream, lights, count,
+                             lpad, m, vlights, nonfinite);
 }
 
 cudaError_t launch_bin(const ViewCull& v, cudaStream_t stream)
 {
     if (v.slices == 0) return cudaSuccess;
-    bin_slices_kernel<<<(v.slices + kBinSlicesSingle - 1) / kBinSlicesSingle, kBinWarpsSingle * 32, 0, stream>>>(v);
-    return cudaGetLastError();
+    return launch_overlapped(bin_slices_kernel, dim3((v.slices + kBinSlicesSingle - 1) / kBinSlicesSingle),
+                             dim3(kBinWarpsSingle * 32), 0, stream, v);
 }
 
 cudaError_t launch_cull(const ViewCull& v, const CullConfig& cfg, uint32_t* dev_error, cudaStream_t stream)
@@ -1397,11 +1432,9 @@ cudaError_t launch_finalize(const ViewCull& v, cudaStream_t stream)
         if (v.total) return cudaMemsetAsync(v.total, 0, sizeof(uint32_t), stream);
         return cudaSuccess;
     }
-    scan_kernel<<<1, kScanThreads, 0, stream>>>(v);
-    const cudaError_t e = cudaGetLastError();
+    const cudaError_t e = launch_overlapped(scan_kernel, dim3(1), dim3(kScanThreads), 0, stream, v);
     if (e != cudaSuccess) return e;
-    copy_kernel<<<v.groups, kCopyThreads, 0, stream>>>(v);
-    return cudaGetLastError();
+    return launch_overlapped(copy_kernel, dim3(v.groups), dim3(kCopyThreads), 0, stream, v);
 }
 
 // ---------------------------------------------------------------------------

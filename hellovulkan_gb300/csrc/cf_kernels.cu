@@ -281,8 +281,12 @@ __global__ void __launch_bounds__(kFlagGranule) batch_xform_kernel(const ViewJob
                                                                    uint32_t n_views, uint32_t* __restrict__ queues,
                                                                    uint32_t n_queues)
 {
-    if (blockIdx.x == 0 && threadIdx.x < n_queues) queues[threadIdx.x] = 0;
+    // the job tables are written by the host before the pass: read them while
+    // the previous kernel of the stream drains
     const uint32_t vi = find_view(prefix, n_views, blockIdx.x);
+    grid_dependency_wait();
+    launch_dependents();
+    if (blockIdx.x == 0 && threadIdx.x < n_queues) queues[threadIdx.x] = 0;
     const ViewJob& j = jobs[vi];
     light_xform_body(j.lights, j.light_count, j.v.lpad, j.view, const_cast<float4*>(j.v.vlights),
                      const_cast<uint32_t*>(j.v.nonfinite), blockIdx.x - __ldg(&prefix[vi]));
@@ -1077,6 +1081,8 @@ __global__ void __launch_bounds__(kBinWarpsBatch * 32, 2) batch_bin_kernel(const
                                                                         uint32_t n_views)
 {
     const uint32_t vi = find_view(prefix, n_views, blockIdx.x);
+    grid_dependency_wait();
+    launch_dependents();
     bin_slices_body<kBinWarpsBatch, kBinSlicesBatch>(jobs[vi].v, blockIdx.x - __ldg(&prefix[vi]));
 }
 
@@ -1148,6 +1154,8 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(const ViewCull v)
 // Batched offset scan: one CTA per view.
 __global__ void __launch_bounds__(kScanThreads) batch_scan_kernel(const ViewJob* __restrict__ jobs)
 {
+    grid_dependency_wait();
+    launch_dependents();
     scan_body(jobs[blockIdx.x].v);
 }
 
@@ -1252,6 +1260,7 @@ __global__ void __launch_bounds__(kCopyWarps * 32) batch_copy_kernel(const ViewJ
                                                                      uint32_t n_views)
 {
     const uint32_t vi = find_view(prefix, n_views, blockIdx.x);
+    grid_dependency_wait();
     copy_body(jobs[vi].v, blockIdx.x - __ldg(&prefix[vi]));
 }
 
@@ -1599,9 +1608,8 @@ cudaError_t launch_cull_batch_t(const BatchCull& b, int ctas, uint32_t* dev_erro
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
         }
-        cull_pipe_kernel<K, WARPS, TILE, STAGES>
-            <<<ctas, (WARPS + 1) * 32, smem, stream>>>(b.jobs, b.items, b.n_items, b.queue, dev_error, ViewCull{});
-        return cudaGetLastError();
+        return launch_overlapped(cull_pipe_kernel<K, WARPS, TILE, STAGES>, dim3(ctas), dim3((WARPS + 1) * 32), smem,
+                                 stream, b.jobs, b.items, b.n_items, b.queue, dev_error, ViewCull{});
     }
 }
 
@@ -1632,16 +1640,16 @@ cudaError_t launch_batch_xform(const ViewJob* jobs, const uint32_t* prefix, uint
     if (blocks == 0) {  // no lights anywhere: only the queues need resetting
         return n_queues ? cudaMemsetAsync(queues, 0, n_queues * sizeof(uint32_t), stream) : cudaSuccess;
     }
-    batch_xform_kernel<<<blocks, kFlagGranule, 0, stream>>>(jobs, prefix, n_views, queues, n_queues);
-    return cudaGetLastError();
+    return launch_overlapped(batch_xform_kernel, dim3(blocks), dim3(kFlagGranule), 0, stream, jobs, prefix, n_views,
+                             queues, n_queues);
 }
 
 cudaError_t launch_batch_bin(const ViewJob* jobs, const uint32_t* prefix, uint32_t n_views, uint32_t blocks,
                              cudaStream_t stream)
 {
     if (blocks == 0) return cudaSuccess;
-    batch_bin_kernel<<<blocks, kBinWarpsBatch * 32, 0, stream>>>(jobs, prefix, n_views);
-    return cudaGetLastError();
+    return launch_overlapped(batch_bin_kernel, dim3(blocks), dim3(kBinWarpsBatch * 32), 0, stream, jobs, prefix,
+                             n_views);
 }
 
 cudaError_t launch_batch_cull(const BatchCull& b, const CullConfig& cfg, int ctas, uint32_t* dev_error,
@@ -1675,16 +1683,15 @@ cudaError_t batch_cull_resident_ctas(const CullConfig& cfg, int* ctas)
 cudaError_t launch_batch_scan(const ViewJob* jobs, uint32_t n_views, cudaStream_t stream)
 {
     if (n_views == 0) return cudaSuccess;
-    batch_scan_kernel<<<n_views, kScanThreads, 0, stream>>>(jobs);
-    return cudaGetLastError();
+    return launch_overlapped(batch_scan_kernel, dim3(n_views), dim3(kScanThreads), 0, stream, jobs);
 }
 
 cudaError_t launch_batch_copy(const ViewJob* jobs, const uint32_t* prefix, uint32_t n_views, uint32_t blocks,
                               cudaStream_t stream)
 {
     if (blocks == 0) return cudaSuccess;
-    batch_copy_kernel<<<blocks, kCopyWarps * 32, 0, stream>>>(jobs, prefix, n_views);
-    return cudaGetLastError();
+    return launch_overlapped(batch_copy_kernel, dim3(blocks), dim3(kCopyWarps * 32), 0, stream, jobs, prefix,
+                             n_views);
 }
 
 uint32_t copy_blocks(uint32_t groups) { return (groups + kCopyWarps - 1) / kCopyWarps; }

@@ -66,7 +66,7 @@ struct CfBatch {
     // device
     cfk::ViewJob* d_jobs = nullptr;
     size_t jobs_cap = 0;
-    uint32_t* d_prefix = nullptr;  // 3 x n: xform, bin, copy
+    uint32_t* d_prefix = nullptr;  // 4 x n: xform, bin (in bin order), copy, bin order
     size_t prefix_cap = 0;
     uint2* d_items = nullptr;
     size_t items_cap = 0;
@@ -149,7 +149,7 @@ int rebuild(CfBatch* b)
     b->jobs.assign(n, cfk::ViewJob{});
     std::vector<size_t> ws_off(n);
     std::vector<cfk::WorkspaceLayout> lay(n);
-    std::vector<uint32_t> prefix(3 * (size_t)n), aabb_prefix(n);
+    std::vector<uint32_t> prefix(4 * (size_t)n), aabb_prefix(n);
     std::vector<cfk::AabbJob> aabb_jobs(n);
     uint32_t ab = 0;
     size_t ws = 0;
@@ -183,14 +183,21 @@ int rebuild(CfBatch* b)
         j.light_count = bv.light_count;
         for (int q = 0; q < 16; ++q) j.view[q] = bv.ubo.cameraView[q];
         prefix[i] = xb;
-        prefix[n + i] = bb;
         prefix[2 * (size_t)n + i] = cb;
         aabb_jobs[i] = cfk::AabbJob{bv.ubo, bv.d_aabbs, 0};
         aabb_prefix[i] = ab;
         ab += (C + 255) / 256;
         xb += cfk::granules(j.v.lpad);
-        bb += cfk::bin_blocks(Z);
         cb += cfk::copy_blocks(groups);
+    }
+    // binning blocks: the views with the most lights first (a block reads all
+    // of its view's lights, so those blocks run longest)
+    uint32_t* const order = prefix.data() + 3 * (size_t)n;
+    for (uint32_t i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order, order + n, [&](uint32_t a, uint32_t c) { return b->jobs[a].light_count > b->jobs[c].light_count; });
+    for (uint32_t r = 0; r < n; ++r) {
+        prefix[n + r] = bb;
+        bb += cfk::bin_blocks(b->jobs[order[r]].v.slices);
     }
     b->xform_blocks = xb;
     b->bin_blocks = bb;
@@ -238,7 +245,7 @@ int rebuild(CfBatch* b)
     }
     b->n_items = (uint32_t)items.size();
     s = grow(reinterpret_cast<void**>(&b->d_jobs), &b->jobs_cap, std::max<size_t>(n, 1) * sizeof(cfk::ViewJob), "batch jobs");
-    if (!s) s = grow(reinterpret_cast<void**>(&b->d_prefix), &b->prefix_cap, std::max<size_t>(3 * (size_t)n, 1) * 4, "batch prefix");
+    if (!s) s = grow(reinterpret_cast<void**>(&b->d_prefix), &b->prefix_cap, std::max<size_t>(4 * (size_t)n, 1) * 4, "batch prefix");
     if (!s) s = grow(reinterpret_cast<void**>(&b->d_items), &b->items_cap, std::max<size_t>(items.size(), 1) * sizeof(uint2), "batch items");
     if (!s) s = grow(reinterpret_cast<void**>(&b->d_aabb_jobs), &b->aabb_jobs_cap, std::max<size_t>(n, 1) * sizeof(cfk::AabbJob), "batch AABB jobs");
     if (!s) s = grow(reinterpret_cast<void**>(&b->d_aabb_prefix), &b->aabb_prefix_cap, std::max<size_t>(n, 1) * 4, "batch AABB prefix");
@@ -261,7 +268,7 @@ int enqueue_batch(CfBatch* b, cudaStream_t st)
     const uint32_t* pb = b->d_prefix + n;
     cudaError_t e = cfk::launch_batch_xform(b->d_jobs, px, n, b->xform_blocks, b->d_queues,
                                             (uint32_t)b->buckets.size(), st);
-    if (e == cudaSuccess) e = cfk::launch_batch_bin(b->d_jobs, pb, n, b->bin_blocks, st);
+    if (e == cudaSuccess) e = cfk::launch_batch_bin(b->d_jobs, pb, b->d_prefix + 3 * (size_t)n, n, b->bin_blocks, st);
     for (size_t q = 0; q < b->buckets.size() && e == cudaSuccess; ++q) {
         const CfBatch::Bucket& bk = b->buckets[q];
         cfk::BatchCull bc{b->d_jobs, b->d_items + bk.item_begin, bk.item_count, b->d_queues + q};

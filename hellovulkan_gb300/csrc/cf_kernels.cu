@@ -1078,12 +1078,16 @@ __global__ void __launch_bounds__(kBinWarpsSingle * 32) bin_slices_kernel(const 
 // Batched binning: block b is slice block b - prefix[v] of view v.
 __global__ void __launch_bounds__(kBinWarpsBatch * 32, 2) batch_bin_kernel(const ViewJob* __restrict__ jobs,
                                                                         const uint32_t* __restrict__ prefix,
+                                                                        const uint32_t* __restrict__ order,
                                                                         uint32_t n_views)
 {
-    const uint32_t vi = find_view(prefix, n_views, blockIdx.x);
+    // block ranges follow `order` (when given), heaviest views first, so
+    // that their long blocks start in the first wave
+    const uint32_t r = find_view(prefix, n_views, blockIdx.x);
+    const uint32_t vi = order ? __ldg(&order[r]) : r;
     grid_dependency_wait();
     launch_dependents();
-    bin_slices_body<kBinWarpsBatch, kBinSlicesBatch>(jobs[vi].v, blockIdx.x - __ldg(&prefix[vi]));
+    bin_slices_body<kBinWarpsBatch, kBinSlicesBatch>(jobs[vi].v, blockIdx.x - __ldg(&prefix[r]));
 }
 
 // ---------------------------------------------------------------------------
@@ -1644,12 +1648,13 @@ cudaError_t launch_batch_xform(const ViewJob* jobs, const uint32_t* prefix, uint
                              queues, n_queues);
 }
 
-cudaError_t launch_batch_bin(const ViewJob* jobs, const uint32_t* prefix, uint32_t n_views, uint32_t blocks,
+cudaError_t launch_batch_bin(const ViewJob* jobs, const uint32_t* prefix, const uint32_t* order, uint32_t n_views,
+                             uint32_t blocks,
                              cudaStream_t stream)
 {
     if (blocks == 0) return cudaSuccess;
     return launch_overlapped(batch_bin_kernel, dim3(blocks), dim3(kBinWarpsBatch * 32), 0, stream, jobs, prefix,
-                             n_views);
+                             order, n_views);
 }
 
 cudaError_t launch_batch_cull(const BatchCull& b, const CullConfig& cfg, int ctas, uint32_t* dev_error,

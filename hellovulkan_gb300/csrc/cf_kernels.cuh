@@ -162,8 +162,9 @@ struct BatchCull {
 constexpr uint32_t kMaxBatchQueues = 256;  // queues a batch_xform launch resets (<= its block size)
 cudaError_t launch_batch_xform(const ViewJob* jobs, const uint32_t* prefix, uint32_t n_views, uint32_t blocks,
                                uint32_t* queues, uint32_t n_queues, cudaStream_t stream);
-cudaError_t launch_batch_bin(const ViewJob* jobs, const uint32_t* prefix, uint32_t n_views, uint32_t blocks,
-                             cudaStream_t stream);
+// order (optional): view index per block range, prefix then follows that order
+cudaError_t launch_batch_bin(const ViewJob* jobs, const uint32_t* prefix, const uint32_t* order, uint32_t n_views,
+                             uint32_t blocks, cudaStream_t stream);
 cudaError_t launch_batch_cull(const BatchCull& b, const CullConfig& cfg, int ctas, uint32_t* dev_error,
                               cudaStream_t stream);
 cudaError_t batch_cull_resident_ctas(const CullConfig& cfg, int* ctas);

@@ -486,7 +486,7 @@ int enqueue_batch(CfServer* s, int slot_i, const LaunchPlan& plan, const std::ve
     if (e == cudaSuccess)
         e = cfk::launch_batch_xform(d_jobs, d_prefix, n, plan.xform_blocks, sl.d_queues,
                                     (uint32_t)plan.buckets.size(), st);
-    if (e == cudaSuccess) e = cfk::launch_batch_bin(d_jobs, d_prefix + n, n, plan.bin_blocks, st);
+    if (e == cudaSuccess) e = cfk::launch_batch_bin(d_jobs, d_prefix + n, nullptr, n, plan.bin_blocks, st);
     for (size_t q = 0; q < plan.buckets.size() && e == cudaSuccess; ++q) {
         const LaunchPlan::Bucket& bk = plan.buckets[q];
         int ctas = 0;

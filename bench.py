@@ -524,8 +524,20 @@ def measure_frustum(stream, reps=50):
             r["reference_hardware"] = "RTX 3070 Mobile, 'less than 25 microseconds' (README.md:63)"
         else:
             gbs = n * 36 / (ms * 1e-3) / 1e9
+            traffic = None
+            try:  # DRAM bytes of one launch at this size, from an ncu capture
+                traffic = json.loads((REPO / "profiles" / "dram_bytes_per_launch.json").read_text())[
+                    "frustum_16M"]["frustum_kernel"] if n == 16 << 20 else None
+            except (OSError, ValueError, KeyError):
+                traffic = None
             r["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
-                             "bytes_per_launch": n * 36, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
+                             "bytes_per_launch": n * 36, "traffic": traffic,
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
+            if traffic:
+                r["roofline"]["traffic_gbs"] = traffic / (ms * 1e-3) / 1e9
+                r["roofline"]["traffic_frac"] = r["roofline"]["traffic_gbs"] / hbm_peak
+                r["roofline"]["note"] = ("36 algorithmic bytes per box; DRAM moves 64 (the 16-byte command's sector "
+                                         "is read to merge the 4-byte store, then written back)")
         out["boxes_%d" % n] = r
         del boxes, cmds
     return out

@@ -762,6 +762,10 @@ def run_ours(args):
         np.array_equal(p[4], o_cells) and np.array_equal(p[5][: o_idx.size], o_idx) for p in pipes)
 
     value = ws * tests_per_view * args.steps / (total_ms * 1e-3)
+    gw = cull_cfg_used[0] * cull_cfg_used[1]
+    X, Y, Z = view.grid
+    groups = Z * -(-(X * Y) // gw) if cull_cfg_used[4] else -(-view.clusters // gw)
+    kernels_per_step = (4 if cull_cfg_used[4] else 3) + (1 if groups > 8192 else 0)
     sm_max = clocks.get("sm_max_mhz") or 2070.0
     fp32_peak = SMS * FP32_LANES_PER_SM * sm_max * 1e6 / 1e12
     peak_note = ("nominal FP32 issue rate, %d SMs x %d lanes x %.0f MHz (no measured FP32 peak exists in "
@@ -843,9 +847,9 @@ def run_ours(args):
                 "one_in_flight_ms_per_step": 1e3 * e2e_serial_s / e2e_steps,
                 "timing": "host clock, pinned host buffers, two pipelines in flight (step i + 1 enqueued before "
                           "the host waits for step i's read-back); one_in_flight: each step waits for its own"},
-        # our kernels per step: light transform, [slice binning,] culling, offset scan, copy; each e2e step
-        # adds the read-back kernel (both e2e runs are timed)
-        "gpu_launches": (5 if cull_cfg_used[4] else 4) * args.steps + (6 if cull_cfg_used[4] else 5) * 2 * e2e_steps,
+        # our kernels per step: light transform, [slice binning,] culling, [offset scan, for views of more
+        # than 8192 cluster groups,] copy; each e2e step adds the read-back kernel (both e2e runs are timed)
+        "gpu_launches": kernels_per_step * args.steps + (kernels_per_step + 1) * 2 * e2e_steps,
         "clocks": clocks,
         "batched": batched,
         "served": served,

@@ -121,6 +121,16 @@ __device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void* src, uin
         : "memory");
 }
 
+// Per-thread asynchronous 16-byte global-to-shared copies (cp.async): a thread
+// waits only for its own copies, so no flag or barrier is involved.
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 // Programmatic dependent launch.  The kernels of one view's step are launched
 // with programmatic stream serialisation, so each may be scheduled while the
 // previous kernel of the stream is still running: it runs only its prologue
@@ -149,6 +159,13 @@ __device__ __forceinline__ float max3f(float a, float b, float c)
 __device__ __forceinline__ bool finite_bits(float x)
 {
     return (__float_as_uint(x) & 0x7f800000u) != 0x7f800000u;
+}
+
+__device__ __forceinline__ uint32_t warp_sum(uint32_t x)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
+    return x;
 }
 
 __device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t x, uint32_t lane)
@@ -281,12 +298,8 @@ __global__ void __launch_bounds__(kFlagGranule) batch_xform_kernel(const ViewJob
                                                                    uint32_t n_views, uint32_t* __restrict__ queues,
                                                                    uint32_t n_queues)
 {
-    // the job tables are written by the host before the pass: read them while
-    // the previous kernel of the stream drains
-    const uint32_t vi = find_view(prefix, n_views, blockIdx.x);
-    grid_dependency_wait();
-    launch_dependents();
     if (blockIdx.x == 0 && threadIdx.x < n_queues) queues[threadIdx.x] = 0;
+    const uint32_t vi = find_view(prefix, n_views, blockIdx.x);
     const ViewJob& j = jobs[vi];
     light_xform_body(j.lights, j.light_count, j.v.lpad, j.view, const_cast<float4*>(j.v.vlights),
                      const_cast<uint32_t*>(j.v.nonfinite), blockIdx.x - __ldg(&prefix[vi]));
@@ -678,7 +691,7 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
         mbar_init_fence();
     }
     __syncthreads();
-    grid_dependency_wait();  // a single view's launch may overlap the binning launch's tail
+    grid_dependency_wait();  // a single view's launch may overlap the binning launch's tail (no-op in a batch)
     launch_dependents();
 
     if (warp == WARPS) {
@@ -937,11 +950,17 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
 // once per SLICES slices (a batch bins 4 slices per 512-thread CTA; a single
 // view, which has few slices, one slice per 1024-thread CTA).  Each step bins
 // WARPS x 128 lights (4 chunks of 32 per warp) with ballot/popc and, per
-// slice, a warp scan of the warps' counts.
+// slice, a warp scan of the warps' counts.  Every thread stages its own four
+// lights of the next step in shared memory with cp.async while it bins the
+// current step (two slots per thread), so the step's global-load latency is
+// hidden behind the previous step's work.
 // ---------------------------------------------------------------------------
 constexpr int kBinChunks = 4;
 constexpr int kBinWarpsSingle = 32, kBinSlicesSingle = 1;
 constexpr int kBinWarpsBatch = 16, kBinSlicesBatch = 4;
+
+// dynamic shared memory of a binning CTA: two slots of kBinChunks lights per thread
+constexpr size_t bin_stage_bytes(int warps) { return 2ull * kBinChunks * (size_t)warps * 32 * sizeof(float4); }
 
 template <int kBinWarps, int kBinSlicesT>
 __device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
@@ -950,10 +969,23 @@ __device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
     __shared__ float s_lo[kBinSlices][kBinWarps], s_hi[kBinSlices][kBinWarps];
     __shared__ uint32_t s_cnt[kBinSlices][kBinWarps];
     __shared__ uint32_t s_nan, s_nonfinite;
+    extern __shared__ __align__(16) float4 bin_stage[];  // [2 slots][kBinChunks][threads]
+    constexpr uint32_t kThreads = kBinWarps * 32;
+    constexpr uint32_t kStep = kBinWarps * kBinChunks * 32;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t xy = v.slice_clusters, k0 = blk * kBinSlices;
     const uint32_t ns = min(kBinSlices, v.slices - k0);
     const float inf = __uint_as_float(0x7f800000u);
+    // this thread's lights of the step at `base` into slot `slot`
+    auto stage = [&](uint32_t base, uint32_t slot) {
+#pragma unroll
+        for (int q = 0; q < kBinChunks; ++q) {
+            const uint32_t i = base + warp * (kBinChunks * 32) + q * 32 + lane;
+            if (i < v.lpad) cp_async16(smem_u32(&bin_stage[(slot * kBinChunks + q) * kThreads + tid]), &v.vlights[i]);
+        }
+        cp_async_commit();
+    };
+    stage(0, 0);  // in flight during the slab reduction
     if (tid == 0) {
         s_nan = 0;
         s_nonfinite = 0;
@@ -1004,14 +1036,21 @@ __device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
     const uint32_t lt_mask = (1u << lane) - 1u;
     uint32_t running[kBinSlices] = {};
     uint32_t nonfinite = 0;  // bit sl: this thread binned a non-finite light into slice sl
-    constexpr uint32_t kStep = kBinWarps * kBinChunks * 32;
-    for (uint32_t base = 0; base < v.lpad; base += kStep) {
+    uint32_t slot = 0;
+    for (uint32_t base = 0; base < v.lpad; base += kStep, slot ^= 1u) {
+        // the other slot was read into registers a step ago, before a barrier
+        if (base + kStep < v.lpad) {
+            stage(base + kStep, slot ^ 1u);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
         float4 L[kBinChunks];
         bool fin[kBinChunks];
 #pragma unroll
         for (int q = 0; q < kBinChunks; ++q) {
             const uint32_t i = base + warp * (kBinChunks * 32) + q * 32 + lane;
-            L[q] = i < v.lpad ? v.vlights[i] : make_float4(0.f, 0.f, 0.f, -inf);
+            L[q] = i < v.lpad ? bin_stage[(slot * kBinChunks + q) * kThreads + tid] : make_float4(0.f, 0.f, 0.f, -inf);
             fin[q] = finite_bits(L[q].x) && finite_bits(L[q].y) && finite_bits(L[q].z);
         }
         uint32_t m[kBinSlices][kBinChunks];
@@ -1085,8 +1124,6 @@ __global__ void __launch_bounds__(kBinWarpsBatch * 32, 2) batch_bin_kernel(const
     // that their long blocks start in the first wave
     const uint32_t r = find_view(prefix, n_views, blockIdx.x);
     const uint32_t vi = order ? __ldg(&order[r]) : r;
-    grid_dependency_wait();
-    launch_dependents();
     bin_slices_body<kBinWarpsBatch, kBinSlicesBatch>(jobs[vi].v, blockIdx.x - __ldg(&prefix[r]));
 }
 
@@ -1158,8 +1195,6 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(const ViewCull v)
 // Batched offset scan: one CTA per view.
 __global__ void __launch_bounds__(kScanThreads) batch_scan_kernel(const ViewJob* __restrict__ jobs)
 {
-    grid_dependency_wait();
-    launch_dependents();
     scan_body(jobs[blockIdx.x].v);
 }
 
@@ -1212,24 +1247,41 @@ __device__ __forceinline__ void copy_body(const ViewCull& v, uint32_t blk)
 // from the staging rows to the packed list, each finding its cluster by a
 // binary search over the exclusive sums, four loads in flight per thread.
 constexpr uint32_t kCopyThreads = 256, kCopyBlockIlp = 4;
+constexpr uint32_t kSumGroupsMax = 8192;  // views with more groups scan their totals in a launch of their own
+// kSumGroups: the view has at most kSumGroupsMax groups and no scan launch
+// ran; each block sums the totals of the groups before its own (from L2/L1,
+// at most kSumGroupsMax / kCopyThreads loads per thread) and the last block
+// writes the view's total.
+template <bool kSumGroups>
 __global__ void __launch_bounds__(kCopyThreads) copy_kernel(const ViewCull v)
 {
     __shared__ uint32_t s_excl[33];
     __shared__ uint32_t s_base;
+    __shared__ uint32_t s_part[kCopyThreads / 32];
     grid_dependency_wait();
     const uint32_t b = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
     uint32_t first, end;
     group_range(v, b, &first, &end);
+    if constexpr (kSumGroups) {
+        uint32_t part = 0;
+        for (uint32_t j = tid; j < b; j += kCopyThreads) part += __ldg(&v.group_sums[j]);
+        part = warp_sum(part);
+        if (lane == 0) s_part[tid >> 5] = part;
+        __syncthreads();
+    }
     if (tid < 32) {
         const uint32_t c = first + lane;
         const uint32_t cnt = c < end ? v.counts[c] : 0u;
         const uint32_t incl = warp_inclusive_scan(cnt, lane);
-        const uint32_t base = v.group_offsets[b];
+        uint32_t base;
+        if constexpr (kSumGroups) base = warp_sum(lane < kCopyThreads / 32 ? s_part[lane] : 0u);
+        else base = v.group_offsets[b];
         if (c < end) v.cells[c] = CfLightCell{base + incl - cnt, cnt};
         s_excl[lane] = incl - cnt;  // lanes past the group hold the group's total
         if (lane == 31) {
             s_excl[32] = incl;
             s_base = base;
+            if (kSumGroups && b == gridDim.x - 1 && v.total) *v.total = base + incl;
         }
     }
     __syncthreads();
@@ -1264,16 +1316,17 @@ __global__ void __launch_bounds__(kCopyWarps * 32) batch_copy_kernel(const ViewJ
                                                                      uint32_t n_views)
 {
     const uint32_t vi = find_view(prefix, n_views, blockIdx.x);
-    grid_dependency_wait();
     copy_body(jobs[vi].v, blockIdx.x - __ldg(&prefix[vi]));
 }
 
-// Launches `kernel` with programmatic stream serialisation (see
-// grid_dependency_wait): it may be scheduled while the stream's previous
-// kernel is still running.
+// Launches `kernel`; with `overlap`, with programmatic stream serialisation
+// (see grid_dependency_wait): it may be scheduled while the stream's previous
+// kernel is still running.  A single view's step uses it.  Batched passes do
+// not: their kernels are long, and with several streams in flight (the
+// server) CTAs launched early would hold SM slots while they wait.
 template <typename... Params, typename... Args>
-cudaError_t launch_overlapped(void (*kernel)(Params...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
-                              Args&&... args)
+cudaError_t launch_kernel(bool overlap, void (*kernel)(Params...), dim3 grid, dim3 block, size_t smem,
+                         cudaStream_t stream, Args&&... args)
 {
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -1283,8 +1336,8 @@ cudaError_t launch_overlapped(void (*kernel)(Params...), dim3 grid, dim3 block, 
     cfg.blockDim = block;
     cfg.dynamicSmemBytes = smem;
     cfg.stream = stream;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.attrs = overlap ? attr : nullptr;
+    cfg.numAttrs = overlap ? 1 : 0;
     return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
@@ -1309,7 +1362,7 @@ cudaError_t launch_cull_t(const ViewCull& v, uint32_t* dev_error, cudaStream_t s
         }();
         if (resident <= 0) return cudaErrorInvalidConfiguration;
         const uint32_t ctas = std::min<uint32_t>(v.groups, (uint32_t)resident);
-        return launch_overlapped(cull_pipe_kernel<K, WARPS, TILE, STAGES>, dim3(ctas), dim3((WARPS + 1) * 32), psmem,
+        return launch_kernel(true, cull_pipe_kernel<K, WARPS, TILE, STAGES>, dim3(ctas), dim3((WARPS + 1) * 32), psmem,
                                  stream, static_cast<const ViewJob*>(nullptr), static_cast<const uint2*>(nullptr),
                                  v.groups, v.queue, dev_error, v);
     } else {
@@ -1319,7 +1372,7 @@ cudaError_t launch_cull_t(const ViewCull& v, uint32_t* dev_error, cudaStream_t s
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
         }
-        return launch_overlapped(cull_kernel<K, WARPS, TILE, STAGES>, dim3(v.groups), dim3((WARPS + 1) * 32), smem,
+        return launch_kernel(true, cull_kernel<K, WARPS, TILE, STAGES>, dim3(v.groups), dim3((WARPS + 1) * 32), smem,
                                  stream, v, dev_error);
     }
 }
@@ -1417,15 +1470,19 @@ cudaError_t launch_light_xform(const CfLightData* lights, uint32_t count, const 
     if (lpad == 0) return cudaSuccess;
     Mat4 m;
     for (int i = 0; i < 16; ++i) m.m[i] = view[i];
-    return launch_overlapped(light_xform_kernel, dim3(granules(lpad)), dim3(kFlagGranule), 0, stream, lights, count,
+    return launch_kernel(true, light_xform_kernel, dim3(granules(lpad)), dim3(kFlagGranule), 0, stream, lights, count,
                              lpad, m, vlights, nonfinite);
 }
 
 cudaError_t launch_bin(const ViewCull& v, cudaStream_t stream)
 {
     if (v.slices == 0) return cudaSuccess;
-    return launch_overlapped(bin_slices_kernel, dim3((v.slices + kBinSlicesSingle - 1) / kBinSlicesSingle),
-                             dim3(kBinWarpsSingle * 32), 0, stream, v);
+    constexpr size_t smem = bin_stage_bytes(kBinWarpsSingle);
+    static const cudaError_t attr =  // one-time opt-in above 48 KB
+        cudaFuncSetAttribute(bin_slices_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (attr != cudaSuccess) return attr;
+    return launch_kernel(true, bin_slices_kernel, dim3((v.slices + kBinSlicesSingle - 1) / kBinSlicesSingle),
+                             dim3(kBinWarpsSingle * 32), smem, stream, v);
 }
 
 cudaError_t launch_cull(const ViewCull& v, const CullConfig& cfg, uint32_t* dev_error, cudaStream_t stream)
@@ -1445,9 +1502,11 @@ cudaError_t launch_finalize(const ViewCull& v, cudaStream_t stream)
         if (v.total) return cudaMemsetAsync(v.total, 0, sizeof(uint32_t), stream);
         return cudaSuccess;
     }
-    const cudaError_t e = launch_overlapped(scan_kernel, dim3(1), dim3(kScanThreads), 0, stream, v);
+    if (v.groups <= kSumGroupsMax)  // each copy block sums the earlier groups' totals itself
+        return launch_kernel(true, copy_kernel<true>, dim3(v.groups), dim3(kCopyThreads), 0, stream, v);
+    const cudaError_t e = launch_kernel(true, scan_kernel, dim3(1), dim3(kScanThreads), 0, stream, v);
     if (e != cudaSuccess) return e;
-    return launch_overlapped(copy_kernel, dim3(v.groups), dim3(kCopyThreads), 0, stream, v);
+    return launch_kernel(true, copy_kernel<false>, dim3(v.groups), dim3(kCopyThreads), 0, stream, v);
 }
 
 // ---------------------------------------------------------------------------
@@ -1612,7 +1671,7 @@ cudaError_t launch_cull_batch_t(const BatchCull& b, int ctas, uint32_t* dev_erro
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
         }
-        return launch_overlapped(cull_pipe_kernel<K, WARPS, TILE, STAGES>, dim3(ctas), dim3((WARPS + 1) * 32), smem,
+        return launch_kernel(false, cull_pipe_kernel<K, WARPS, TILE, STAGES>, dim3(ctas), dim3((WARPS + 1) * 32), smem,
                                  stream, b.jobs, b.items, b.n_items, b.queue, dev_error, ViewCull{});
     }
 }
@@ -1644,7 +1703,7 @@ cudaError_t launch_batch_xform(const ViewJob* jobs, const uint32_t* prefix, uint
     if (blocks == 0) {  // no lights anywhere: only the queues need resetting
         return n_queues ? cudaMemsetAsync(queues, 0, n_queues * sizeof(uint32_t), stream) : cudaSuccess;
     }
-    return launch_overlapped(batch_xform_kernel, dim3(blocks), dim3(kFlagGranule), 0, stream, jobs, prefix, n_views,
+    return launch_kernel(false, batch_xform_kernel, dim3(blocks), dim3(kFlagGranule), 0, stream, jobs, prefix, n_views,
                              queues, n_queues);
 }
 
@@ -1653,7 +1712,11 @@ cudaError_t launch_batch_bin(const ViewJob* jobs, const uint32_t* prefix, const 
                              cudaStream_t stream)
 {
     if (blocks == 0) return cudaSuccess;
-    return launch_overlapped(batch_bin_kernel, dim3(blocks), dim3(kBinWarpsBatch * 32), 0, stream, jobs, prefix,
+    constexpr size_t smem = bin_stage_bytes(kBinWarpsBatch);
+    static const cudaError_t attr =  // one-time opt-in above 48 KB
+        cudaFuncSetAttribute(batch_bin_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (attr != cudaSuccess) return attr;
+    return launch_kernel(false, batch_bin_kernel, dim3(blocks), dim3(kBinWarpsBatch * 32), smem, stream, jobs, prefix,
                              order, n_views);
 }
 
@@ -1688,14 +1751,14 @@ cudaError_t batch_cull_resident_ctas(const CullConfig& cfg, int* ctas)
 cudaError_t launch_batch_scan(const ViewJob* jobs, uint32_t n_views, cudaStream_t stream)
 {
     if (n_views == 0) return cudaSuccess;
-    return launch_overlapped(batch_scan_kernel, dim3(n_views), dim3(kScanThreads), 0, stream, jobs);
+    return launch_kernel(false, batch_scan_kernel, dim3(n_views), dim3(kScanThreads), 0, stream, jobs);
 }
 
 cudaError_t launch_batch_copy(const ViewJob* jobs, const uint32_t* prefix, uint32_t n_views, uint32_t blocks,
                               cudaStream_t stream)
 {
     if (blocks == 0) return cudaSuccess;
-    return launch_overlapped(batch_copy_kernel, dim3(blocks), dim3(kCopyWarps * 32), 0, stream, jobs, prefix,
+    return launch_kernel(false, batch_copy_kernel, dim3(blocks), dim3(kCopyWarps * 32), 0, stream, jobs, prefix,
                              n_views);
 }
 

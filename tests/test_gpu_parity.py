@@ -72,6 +72,16 @@ def test_dense_slices_with_a_short_last_group(gpu, oracle, tuning):
     assert_matches_oracle(oracle, v, *run_pipeline(gpu, v, tuning))
 
 
+@pytest.mark.parametrize("tuning", [(1, 4, 512, 4, 0), (1, 4, 256, 4, 1), (2, 8, 1024, 2, 1)])
+def test_offsets_with_and_without_a_scan_launch(gpu, oracle, tuning):
+    """Views of more than 8192 cluster groups scan the group totals in a launch
+    of their own; smaller ones let each copy block sum the earlier groups."""
+    rng = np.random.default_rng(23)
+    v = scenes.custom_view((64, 36, 24), 3840, 2160, 0.1, 500.0,
+                           lights=scenes.uniform_box_lights(rng, 600, [-40, -20, -150], [40, 20, -1], 1.0, 6.0))
+    assert_matches_oracle(oracle, v, *run_pipeline(gpu, v, tuning))
+
+
 def test_read_outputs_into_pinned_memory(gpu, oracle):
     """The one-launch read-back into pinned host buffers gives what the
     two-copy path gives: the full lists, and a prefix for a short index buffer."""

@@ -95,6 +95,17 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(values, device="cpu"):
+    """Per-rank timings reduced to the slowest rank's (the whole job ends when
+    its last replica does); the identity with one process."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x) for x in values], dtype=torch.float64, device=device)
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 # --------------------------------------------------------------------------- clocks
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
@@ -744,10 +755,7 @@ def run_ours(args):
                                                     batched["per_view_launch_views_per_s"])
 
     tests_per_view = view.clusters * view.light_count
-    stats = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device="cuda")
-    if ws > 1:
-        torch.distributed.all_reduce(stats, op=torch.distributed.ReduceOp.MAX)
-    total_ms, e2e_s = float(stats[0]), float(stats[1])
+    total_ms, e2e_s = max_over_ranks([total_ms, e2e_s], device="cuda")
     if rank != 0:
         torch.distributed.destroy_process_group()
         return

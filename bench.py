@@ -16,7 +16,8 @@ ours       value: device-resident inputs, each step timed with CUDA events on
            the launching stream, L2 flushed (256 MiB write) between steps.
            e2e:   the same step through the C ABI with host buffers: pinned
            LightData upload, the pipeline call, and the LightCell + index
-           read-back, timed on the host clock with synchronisation.
+           read-back into pinned memory, timed on the host clock, with two
+           pipelines in flight (and with one, reported beside it).
            roofline: the culling kernel's own event-timed duration against the
            FP32 issue rate (16 ops per executed test).
            cpu_baseline: the reference's LightCulling.comp compiled as C++

@@ -221,6 +221,7 @@ int rebuild(CfBatch* b)
         j.v.slice_idx = reinterpret_cast<uint32_t*>(w + L.slice_idx);
         j.v.slice_count = reinterpret_cast<uint32_t*>(w + L.slice_count);
         j.v.slice_nonfinite = reinterpret_cast<uint32_t*>(w + L.slice_nonfinite);
+        j.v.group_boxes = reinterpret_cast<float4*>(w + L.group_boxes);
     }
     // buckets and items: views by decreasing light count, groups in order
     std::map<uint32_t, std::vector<uint32_t>> by_key;

@@ -623,23 +623,24 @@ static_assert(sizeof(ItemDesc) % 16 == 0, "descriptor slots stay 16-byte aligned
 constexpr uint32_t kItemTerminate = 1u, kItemExact = 2u;
 
 // Dynamic shared memory of cull_pipe_kernel: stage tiles and their light
-// indices, kItemSlots groups of AABBs, the survivor buffer, kItemSlots
-// descriptors, the mbarriers, then small words.
+// indices, kItemSlots groups of AABBs and their union boxes, the survivor
+// buffer, kItemSlots descriptors, the mbarriers, then small words.
 template <int K, int WARPS, int TILE, int STAGES>
 struct PipeSmem {
     static constexpr uint32_t kGroup = (uint32_t)(K * WARPS);
     static constexpr size_t tiles = 0;
     static constexpr size_t idx = tiles + (size_t)STAGES * TILE * sizeof(float4);
     static constexpr size_t boxes = idx + (size_t)STAGES * TILE * sizeof(uint32_t);
-    static constexpr size_t surv_l = boxes + (size_t)kItemSlots * kGroup * sizeof(CfAABB);
+    static constexpr size_t ubox = boxes + (size_t)kItemSlots * kGroup * sizeof(CfAABB);  // the group's union, per slot
+    static constexpr size_t surv_l = ubox + (size_t)kItemSlots * sizeof(CfAABB);
     static constexpr size_t surv_i = surv_l + (size_t)TILE * sizeof(float4);
     static constexpr size_t desc = surv_i + (size_t)TILE * sizeof(uint32_t);
     static constexpr size_t bars = desc + kItemSlots * sizeof(ItemDesc);
     static constexpr size_t small = bars + (2 * STAGES + 2 * kItemSlots) * sizeof(uint64_t);
-    // stop[STAGES], done[kItemSlots], chunk counts[TILE / 32], boxes[WARPS * 8], warp sums[WARPS], the
-    // consumers' abort flag, the producer's abort flag
-    static constexpr size_t bytes = small + (STAGES + kItemSlots + TILE / 32 + WARPS * 8 + WARPS + 2) * 4;
-    static_assert(boxes % 16 == 0 && desc % 16 == 0 && bars % 8 == 0, "shared-memory alignment");
+    // stop[STAGES], done[kItemSlots], chunk counts[TILE / 32], warp sums[WARPS], the consumers' abort
+    // flag, the producer's abort flag
+    static constexpr size_t bytes = small + (STAGES + kItemSlots + TILE / 32 + WARPS + 2) * 4;
+    static_assert(boxes % 16 == 0 && ubox % 16 == 0 && desc % 16 == 0 && bars % 8 == 0, "shared-memory alignment");
 };
 
 template <int K, int WARPS, int TILE, int STAGES>
@@ -655,6 +656,7 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
     float4* const tiles = reinterpret_cast<float4*>(smem + Lay::tiles);
     uint32_t* const idx_tiles = reinterpret_cast<uint32_t*>(smem + Lay::idx);
     float4* const boxes = reinterpret_cast<float4*>(smem + Lay::boxes);
+    const float4* const uboxes = reinterpret_cast<const float4*>(smem + Lay::ubox);
     float4* const surv_l = reinterpret_cast<float4*>(smem + Lay::surv_l);
     uint32_t* const surv_i = reinterpret_cast<uint32_t*>(smem + Lay::surv_i);
     ItemDesc* const desc = reinterpret_cast<ItemDesc*>(smem + Lay::desc);
@@ -665,8 +667,7 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
     volatile uint32_t* const stop = reinterpret_cast<volatile uint32_t*>(smem + Lay::small);
     uint32_t* const done = const_cast<uint32_t*>(stop) + STAGES;  // per slot: consumer warps all capped
     uint32_t* const s_cnt = done + kItemSlots;
-    float* const s_box = reinterpret_cast<float*>(s_cnt + TILE / 32);
-    uint32_t* const s_gsum = reinterpret_cast<uint32_t*>(s_box + WARPS * 8);
+    uint32_t* const s_gsum = s_cnt + TILE / 32;
     // s_abort is written only by consumer threads, before a consumer barrier,
     // so every consumer warp reads the same value after it; the producer
     // keeps its own flag and the consumers learn of its failure through their
@@ -737,9 +738,11 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
             d.cap = v.cap;
             d.flags = v.slice_nonfinite[k] ? kItemExact : 0u;
             done[r] = 0;
-            mbar_arrive_expect_tx(smem_u32(&ifull[r]), nb * (uint32_t)sizeof(CfAABB));
+            mbar_arrive_expect_tx(smem_u32(&ifull[r]), (nb + 1) * (uint32_t)sizeof(CfAABB));
             bulk_copy_g2s(smem_u32(boxes + (size_t)r * kGroup * 2), v.aabbs + 2 * (size_t)first,
                           nb * (uint32_t)sizeof(CfAABB), smem_u32(&ifull[r]));
+            bulk_copy_g2s(smem_u32(uboxes + (size_t)r * 2), v.group_boxes + 2 * (size_t)item.y,
+                          (uint32_t)sizeof(CfAABB), smem_u32(&ifull[r]));
             filled = n + 1;
             const float4* src = v.slice_lights + (size_t)k * v.lpad;
             const uint32_t* src_idx = v.slice_idx + (size_t)k * v.lpad;
@@ -832,23 +835,7 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
                 w.umx[a] = inf;
             }
         }
-        if (lane == 0) {
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                s_box[warp * 8 + a] = w.umn[a];
-                s_box[warp * 8 + 3 + a] = w.umx[a];
-            }
-            if (wdone) atomicAdd(&done[r], 1u);
-        }
-        consumer_sync<WARPS * 32>();
-        float cmn[3] = {inf, inf, inf}, cmx[3] = {-inf, -inf, -inf};
-        for (int q = 0; q < WARPS; ++q) {
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                cmn[a] = fminf(cmn[a], s_box[q * 8 + a]);
-                cmx[a] = fmaxf(cmx[a], s_box[q * 8 + 3 + a]);
-            }
-        }
+        if (lane == 0 && wdone) atomicAdd(&done[r], 1u);
         const bool exact = (d.flags & kItemExact) != 0;
         uint32_t chunks_filtered = 0, chunks_tested = 0;
         for (uint32_t t = 0; t < d.ntiles; ++t) {
@@ -867,6 +854,10 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
             const uint32_t cnt = min((uint32_t)TILE, d.nsrc - t * TILE);
             const float4* tile = tiles + (size_t)s * TILE;
             const uint32_t* itile = idx_tiles + (size_t)s * TILE;
+            // the group's union box (binning launch; infinite when a bound is NaN), read per tile so that
+            // it is not held in registers across the loop
+            const float4 ulo = uboxes[2 * r], uhi = uboxes[2 * r + 1];
+            const float cmn[3] = {ulo.x, ulo.y, ulo.z}, cmx[3] = {uhi.x, uhi.y, uhi.z};
             float4 Ls[kPer];
             uint32_t Is[kPer], Ms[kPer];
 #pragma unroll
@@ -1030,6 +1021,43 @@ __device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
         if ((s_nan >> sl) & 1u) {
             lo[sl] = -inf;
             hi[sl] = inf;
+        }
+    }
+
+    // The union box of every cluster group of these slices, the culling
+    // kernel's filter box: lanes of a warp hold consecutive clusters, and a
+    // group (a power of two <= 32 wide) is an aligned run of lanes, reduced
+    // with xor shuffles.  A NaN bound makes the group's box infinite.
+    if (v.group_boxes) {
+        const uint32_t gw = v.group_width, gps = (xy + gw - 1) / gw;
+        for (uint32_t sl = 0; sl < ns; ++sl) {
+            const size_t c0 = (size_t)(k0 + sl) * xy;
+            for (uint32_t cb = 0; cb < gps * gw; cb += kThreads) {
+                const uint32_t c = cb + tid;
+                float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
+                bool nan = false;
+                if (c < xy) {
+                    const float4 a = v.aabbs[2 * (c0 + c)], b = v.aabbs[2 * (c0 + c) + 1];
+                    lo[0] = a.x; lo[1] = a.y; lo[2] = a.z;
+                    hi[0] = b.x; hi[1] = b.y; hi[2] = b.z;
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) nan |= (lo[q] != lo[q]) | (hi[q] != hi[q]);
+                }
+                for (uint32_t o = 1; o < gw; o <<= 1) {
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        lo[q] = fminf(lo[q], __shfl_xor_sync(kFull, lo[q], o));
+                        hi[q] = fmaxf(hi[q], __shfl_xor_sync(kFull, hi[q], o));
+                    }
+                }
+                const uint32_t seg = gw == 32 ? kFull : ((1u << gw) - 1u) << (lane & ~(gw - 1));
+                nan = (__ballot_sync(kFull, nan) & seg) != 0;
+                if (c < gps * gw && (lane & (gw - 1)) == 0) {
+                    const size_t g = (size_t)(k0 + sl) * gps + c / gw;
+                    v.group_boxes[2 * g] = nan ? make_float4(-inf, -inf, -inf, 0.f) : make_float4(lo[0], lo[1], lo[2], 0.f);
+                    v.group_boxes[2 * g + 1] = nan ? make_float4(inf, inf, inf, 0.f) : make_float4(hi[0], hi[1], hi[2], 0.f);
+                }
+            }
         }
     }
 
@@ -1450,6 +1478,8 @@ WorkspaceLayout workspace_layout(uint32_t clusters, uint32_t lights, uint32_t ca
         off += al((size_t)slices * sizeof(uint32_t));
         w.slice_nonfinite = off;
         off += al((size_t)slices * sizeof(uint32_t));
+        w.group_boxes = off;
+        off += al((size_t)groups * 2 * sizeof(float4));
     }
     w.bytes = off;
     return w;

@@ -50,6 +50,7 @@ struct ViewCull {
     uint32_t* slice_idx;
     uint32_t* slice_count;      // padded length of each slice's list
     uint32_t* slice_nonfinite;  // 1 when a listed light has a non-finite coordinate
+    float4* group_boxes;        // per cluster group, the union of its AABBs (lo, hi; NaN bound: infinite)
     // optional work counters (profiling only, null otherwise): [0] sphere-box
     // tests against slice slabs and warp union boxes, [1] sphere-box tests
     // against cluster boxes
@@ -114,7 +115,7 @@ struct CullConfig {
 // Workspace carve-up for one view (cf_cull_lights).
 struct WorkspaceLayout {
     size_t vlights, nonfinite, counts, staging, group_sums, group_offsets, slice_lights, slice_idx, slice_count,
-        slice_nonfinite, bytes;
+        slice_nonfinite, group_boxes, bytes;
 };
 constexpr size_t kQueueWord = 64;  // byte offset, in a workspace's status block, of the single-view item counter
 // Scratch of one view; `groups` = group_count(...) of the configuration used.

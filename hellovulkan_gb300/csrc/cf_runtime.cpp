@@ -167,6 +167,7 @@ int enqueue_cull(const CfClusterForwardUBO& ubo, const CfAABB* d_aabbs, const Cf
         v.slice_idx = reinterpret_cast<uint32_t*>(ws + L.slice_idx);
         v.slice_count = reinterpret_cast<uint32_t*>(ws + L.slice_count);
         v.slice_nonfinite = reinterpret_cast<uint32_t*>(ws + L.slice_nonfinite);
+        v.group_boxes = reinterpret_cast<float4*>(ws + L.group_boxes);
         v.queue = reinterpret_cast<uint32_t*>(ws + cfk::kQueueWord);
     }
     cudaError_t e = stage_events ? cudaEventRecord(stage_events[0], stream) : cudaSuccess;

@@ -421,6 +421,7 @@ void plan_batch(CfServer* s, int slot_i, const std::vector<Request*>& reqs, Laun
         j.v.slice_idx = reinterpret_cast<uint32_t*>(w + L.slice_idx);
         j.v.slice_count = reinterpret_cast<uint32_t*>(w + L.slice_count);
         j.v.slice_nonfinite = reinterpret_cast<uint32_t*>(w + L.slice_nonfinite);
+        j.v.group_boxes = reinterpret_cast<float4*>(w + L.group_boxes);
         j.v.group_sums = reinterpret_cast<uint32_t*>(w + L.group_sums);
         j.v.group_offsets = reinterpret_cast<uint32_t*>(w + L.group_offsets);
         j.v.lpad = cfk::pad_lights(r->lights->count);

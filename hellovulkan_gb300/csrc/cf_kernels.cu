@@ -983,18 +983,48 @@ __device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
         if (k0 == 0 && v.queue) *v.queue = 0u;  // the single-view culling launch's item counter
     }
     __syncthreads();
+    // One pass over each slice's cluster AABBs: the slab (lowest min.z,
+    // highest max.z) and the union box of every cluster group, the culling
+    // kernel's filter box.  Lanes of a warp hold consecutive clusters, so a
+    // group (a power of two <= 32 wide) is an aligned run of lanes, reduced
+    // with xor shuffles.  A NaN bound makes the slab, or the group's box,
+    // infinite.
+    const uint32_t gw = v.group_width, gps = (xy + gw - 1) / gw;
+    const uint32_t span = v.group_boxes ? gps * gw : xy;  // clusters a pass covers (groups padded)
 #pragma unroll
     for (uint32_t sl = 0; sl < kBinSlices; ++sl) {
         float lo = inf, hi = -inf;
         bool nan = false;
         if (sl < ns) {
             const size_t c0 = (size_t)(k0 + sl) * xy;
-            for (uint32_t c = tid; c < xy; c += kBinWarps * 32) {
-                const float a = v.aabbs[2 * (c0 + c)].z;
-                const float b = v.aabbs[2 * (c0 + c) + 1].z;
-                nan |= (a != a) | (b != b);
-                lo = fminf(lo, a);
-                hi = fmaxf(hi, b);
+            for (uint32_t cb = 0; cb < span; cb += kThreads) {  // uniform trip count: the shuffles below
+                const uint32_t c = cb + tid;
+                float4 a = make_float4(inf, inf, inf, 0.f), b = make_float4(-inf, -inf, -inf, 0.f);
+                if (c < xy) {
+                    a = v.aabbs[2 * (c0 + c)];
+                    b = v.aabbs[2 * (c0 + c) + 1];
+                    nan |= (a.z != a.z) | (b.z != b.z);
+                    lo = fminf(lo, a.z);
+                    hi = fmaxf(hi, b.z);
+                }
+                if (v.group_boxes) {
+                    bool gnan = (a.x != a.x) | (a.y != a.y) | (a.z != a.z) | (b.x != b.x) | (b.y != b.y) | (b.z != b.z);
+                    for (uint32_t o = 1; o < gw; o <<= 1) {
+                        a.x = fminf(a.x, __shfl_xor_sync(kFull, a.x, o));
+                        a.y = fminf(a.y, __shfl_xor_sync(kFull, a.y, o));
+                        a.z = fminf(a.z, __shfl_xor_sync(kFull, a.z, o));
+                        b.x = fmaxf(b.x, __shfl_xor_sync(kFull, b.x, o));
+                        b.y = fmaxf(b.y, __shfl_xor_sync(kFull, b.y, o));
+                        b.z = fmaxf(b.z, __shfl_xor_sync(kFull, b.z, o));
+                    }
+                    const uint32_t seg = gw == 32 ? kFull : ((1u << gw) - 1u) << (lane & ~(gw - 1));
+                    gnan = (__ballot_sync(kFull, gnan) & seg) != 0;
+                    if (c < gps * gw && (lane & (gw - 1)) == 0) {
+                        const size_t g = (size_t)(k0 + sl) * gps + c / gw;
+                        v.group_boxes[2 * g] = gnan ? make_float4(-inf, -inf, -inf, 0.f) : make_float4(a.x, a.y, a.z, 0.f);
+                        v.group_boxes[2 * g + 1] = gnan ? make_float4(inf, inf, inf, 0.f) : make_float4(b.x, b.y, b.z, 0.f);
+                    }
+                }
             }
         }
 #pragma unroll
@@ -1021,43 +1051,6 @@ __device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
         if ((s_nan >> sl) & 1u) {
             lo[sl] = -inf;
             hi[sl] = inf;
-        }
-    }
-
-    // The union box of every cluster group of these slices, the culling
-    // kernel's filter box: lanes of a warp hold consecutive clusters, and a
-    // group (a power of two <= 32 wide) is an aligned run of lanes, reduced
-    // with xor shuffles.  A NaN bound makes the group's box infinite.
-    if (v.group_boxes) {
-        const uint32_t gw = v.group_width, gps = (xy + gw - 1) / gw;
-        for (uint32_t sl = 0; sl < ns; ++sl) {
-            const size_t c0 = (size_t)(k0 + sl) * xy;
-            for (uint32_t cb = 0; cb < gps * gw; cb += kThreads) {
-                const uint32_t c = cb + tid;
-                float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
-                bool nan = false;
-                if (c < xy) {
-                    const float4 a = v.aabbs[2 * (c0 + c)], b = v.aabbs[2 * (c0 + c) + 1];
-                    lo[0] = a.x; lo[1] = a.y; lo[2] = a.z;
-                    hi[0] = b.x; hi[1] = b.y; hi[2] = b.z;
-#pragma unroll
-                    for (int q = 0; q < 3; ++q) nan |= (lo[q] != lo[q]) | (hi[q] != hi[q]);
-                }
-                for (uint32_t o = 1; o < gw; o <<= 1) {
-#pragma unroll
-                    for (int q = 0; q < 3; ++q) {
-                        lo[q] = fminf(lo[q], __shfl_xor_sync(kFull, lo[q], o));
-                        hi[q] = fmaxf(hi[q], __shfl_xor_sync(kFull, hi[q], o));
-                    }
-                }
-                const uint32_t seg = gw == 32 ? kFull : ((1u << gw) - 1u) << (lane & ~(gw - 1));
-                nan = (__ballot_sync(kFull, nan) & seg) != 0;
-                if (c < gps * gw && (lane & (gw - 1)) == 0) {
-                    const size_t g = (size_t)(k0 + sl) * gps + c / gw;
-                    v.group_boxes[2 * g] = nan ? make_float4(-inf, -inf, -inf, 0.f) : make_float4(lo[0], lo[1], lo[2], 0.f);
-                    v.group_boxes[2 * g + 1] = nan ? make_float4(inf, inf, inf, 0.f) : make_float4(hi[0], hi[1], hi[2], 0.f);
-                }
-            }
         }
     }
 

@@ -70,6 +70,7 @@ def parse():
     p.add_argument("--stress-lights", type=int, default=4096)
     p.add_argument("--stress-frames", type=int, default=600)
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline budget")
+    p.add_argument("--e2e-in-flight", type=int, default=2, help="pipelines (frames) in flight in the e2e loop")
     return p.parse_args()
 
 
@@ -661,25 +662,28 @@ def run_ours(args):
 
     # e2e through the C ABI with host buffers: every step uploads its lights
     # from pinned memory, culls, and reads its cells and indices back into
-    # pinned memory.  Two pipelines (resources, culling pipeline, stream) are
-    # in flight, as a renderer double-buffers frames: step i + 1 is enqueued
+    # pinned memory.  k pipelines (resources, culling pipeline, stream) are in
+    # flight, as a renderer keeps frames in flight: step i + k - 1 is enqueued
     # before the host waits for step i's result.
     b = rc.buffers()
     h_lights = torch.from_numpy(np.ascontiguousarray(view.lights)).pin_memory()
-    rl2 = ResourcesLight(ctx)
-    rl2.add_lights(view.lights)
-    rc2 = ResourcesClusterForward(ctx)
-    rc2.create_buffers(*view.grid, view.cap)
-    gen2 = PipelineAABBGenerator(ctx, rc2)
-    gen2.set_cluster_forward_ubo(view.ubo)
-    gen2.fill_command_buffer(stream)
-    cull2 = PipelineLightCulling(ctx, rl2, rc2)
-    if args.tuning:
-        cull2.set_tuning(*[int(t) for t in args.tuning.split(",")])
-    stream2 = torch.cuda.Stream()
+    in_flight = max(2, args.e2e_in_flight)
+    sets = [(rl, rc, cull, stream)]
+    for _ in range(in_flight - 1):
+        rl2 = ResourcesLight(ctx)
+        rl2.add_lights(view.lights)
+        rc2 = ResourcesClusterForward(ctx)
+        rc2.create_buffers(*view.grid, view.cap)
+        gen2 = PipelineAABBGenerator(ctx, rc2)
+        gen2.set_cluster_forward_ubo(view.ubo)
+        gen2.fill_command_buffer(stream)
+        cull2 = PipelineLightCulling(ctx, rl2, rc2)
+        if args.tuning:
+            cull2.set_tuning(*[int(t) for t in args.tuning.split(",")])
+        sets.append((rl2, rc2, cull2, torch.cuda.Stream()))
     pinned = []
     pipes = []
-    for p_rl, p_rc, p_cull, p_st in ((rl, rc, cull, stream), (rl2, rc2, cull2, stream2)):
+    for p_rl, p_rc, p_cull, p_st in sets:
         hc = torch.empty((b.cluster_count, 2), dtype=torch.int32).pin_memory()
         hi = torch.empty(b.index_capacity, dtype=torch.int32).pin_memory()
         pinned += [hc, hi]
@@ -693,22 +697,19 @@ def run_ours(args):
         p_cull.set_cluster_forward_ubo(view.ubo)
         p_cull.fill_command_buffer(p_st)
 
-    def e2e_run(n, in_flight):
+    def e2e_run(n, k):
+        """n steps with k pipelines in flight (k = 1: each step waits for its own)."""
         got = None
-        if in_flight == 1:
-            for _ in range(n):
-                enqueue(pipes[0])
-                _, got = pipes[0][1].read_outputs(pipes[0][3], pipes[0][4], pipes[0][5])
-            return got
-        enqueue(pipes[0])
+        for i in range(min(k - 1, n)):
+            enqueue(pipes[i])
         for i in range(n):
-            if i + 1 < n:
-                enqueue(pipes[(i + 1) % 2])
-            p = pipes[i % 2]
+            if i + k - 1 < n:
+                enqueue(pipes[(i + k - 1) % k])
+            p = pipes[i % k]
             _, got = p[1].read_outputs(p[3], p[4], p[5])
         return got
 
-    e2e_run(4, 2)
+    e2e_run(2 * in_flight, in_flight)
     e2e_run(3, 1)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -716,7 +717,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_serial_s = time.perf_counter() - t0
     t0 = time.perf_counter()
-    got = e2e_run(e2e_steps, 2)
+    got = e2e_run(e2e_steps, in_flight)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     total_indices = got.size
@@ -854,8 +855,10 @@ def run_ours(args):
         "e2e": {"value": ws * tests_per_view * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": bi,
                 "d2h_bytes_per_step": bo, "ms_per_step": 1e3 * e2e_s / e2e_steps, "steps": e2e_steps,
                 "one_in_flight_ms_per_step": 1e3 * e2e_serial_s / e2e_steps,
-                "timing": "host clock, pinned host buffers, two pipelines in flight (step i + 1 enqueued before "
-                          "the host waits for step i's read-back); one_in_flight: each step waits for its own"},
+                "in_flight": in_flight,
+                "timing": "host clock, pinned host buffers, %d pipelines in flight (step i + %d enqueued before "
+                          "the host waits for step i's read-back); one_in_flight: each step waits for its own" % (
+                              in_flight, in_flight - 1)},
         # our kernels per step: light transform, [slice binning,] culling, [offset scan, for views of more
         # than 8192 cluster groups,] copy; each e2e step adds the read-back kernel (both e2e runs are timed)
         "gpu_launches": kernels_per_step * args.steps + (kernels_per_step + 1) * 2 * e2e_steps,

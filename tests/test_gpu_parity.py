@@ -82,6 +82,47 @@ def test_offsets_with_and_without_a_scan_launch(gpu, oracle, tuning):
     assert_matches_oracle(oracle, v, *run_pipeline(gpu, v, tuning))
 
 
+@pytest.mark.parametrize("tuning", [None, (1, 8, 512, 4, 0)])
+def test_single_view_step_replayed_from_a_cuda_graph(gpu, oracle, tuning):
+    """A caller may capture a step (launched with programmatic dependent
+    launch) into a CUDA graph and replay it over new light positions."""
+    import torch
+    from hellovulkan_gb300.pipelines import (PipelineAABBGenerator, PipelineLightCulling, ResourcesClusterForward,
+                                             ResourcesLight)
+    v = scenes.plain_large(5, n_lights=6000)
+    rl = ResourcesLight(gpu)
+    rl.add_lights(v.lights)
+    rc = ResourcesClusterForward(gpu)
+    rc.create_buffers(*v.grid, v.cap)
+    gen = PipelineAABBGenerator(gpu, rc)
+    gen.set_cluster_forward_ubo(v.ubo)
+    gen.fill_command_buffer()
+    cull = PipelineLightCulling(gpu, rl, rc)
+    if tuning:
+        cull.set_tuning(*tuning)
+    cull.set_cluster_forward_ubo(v.ubo)
+    cull.fill_command_buffer()  # outside the capture: workspace and kernel attributes
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        cull.fill_command_buffer(torch.cuda.current_stream())
+    aabbs = oracle.generate_aabbs(v.ubo)
+    rng = np.random.default_rng(31)
+    for _ in range(2):
+        moved = v.lights.copy()
+        moved[:, :3] += rng.normal(0.0, 2.0, size=(moved.shape[0], 3)).astype(np.float32)
+        host = torch.from_numpy(moved).pin_memory()
+        rl.upload_async(host, moved.shape[0], torch.cuda.current_stream())
+        g.replay()
+        torch.cuda.synchronize()
+        cells, idx = rc.read_outputs()
+        oc, oi, _ = oracle.cull(v.ubo, aabbs, moved, v.cap)
+        assert np.array_equal(cells, oc) and np.array_equal(idx, oi)
+    assert gpu.check_device_error() == 0
+    for o in (cull, gen, rc, rl):
+        o.close()
+
+
 def test_read_outputs_into_pinned_memory(gpu, oracle):
     """The one-launch read-back into pinned host buffers gives what the
     two-copy path gives: the full lists, and a prefix for a short index buffer."""

@@ -357,9 +357,9 @@ def measure_batch(ctx, stream, n_views=256, passes=20, seed=3, sample_views=6):
     }
 
 
-def measure_serve(ctx, seconds, rates=(2000.0, 10000.0, 50000.0), sweep=(20000.0, 30000.0, 40000.0, 50000.0,
-                                                                        60000.0, 80000.0),
-                  sweep_seconds=3.0, submit_threads=4):
+def measure_serve(ctx, seconds, rates=(2000.0, 10000.0, 50000.0), sweep=(20000.0, 40000.0, 60000.0, 80000.0,
+                                                                        100000.0, 120000.0, 150000.0, 200000.0),
+                  sweep_seconds=5.0, submit_threads=4):
     """The served stream: Poisson arrivals at each rate for `seconds`, requests
     drawn like the batched mix (4 projections, random cameras, 128 base light
     sets of 256..65536 blob lights), light sets re-referenced with p = 0.7 and
@@ -392,7 +392,7 @@ def measure_serve(ctx, seconds, rates=(2000.0, 10000.0, 50000.0), sweep=(20000.0
     runs = [one(r, seconds, submit_threads) for r in rates]
     swept, best = [], 0.0
     for r in sweep:
-        x = one(r, sweep_seconds, 8)
+        x = one(r, sweep_seconds, submit_threads)
         swept.append({k: x[k] for k in ("rate", "achieved_rate", "latency_p50_ms", "latency_p99_ms",
                                          "mean_views_per_batch", "sustained")})
         if not x["sustained"]:

@@ -685,7 +685,13 @@ int cf_server_create(CfContext* ctx, const CfServerConfig* config, CfServer** ou
     s->t0 = now_s();
     DeviceGuard g(s->device);
     cudaError_t e = cudaMalloc(&s->d_pool, c.hbm_budget_bytes);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->upload, cudaStreamNonBlocking);
+    // The upload stream (light-set copies and jitters) at the highest priority:
+    // the batch streams' persistent culling launches fill every SM, and its
+    // small kernels must be scheduled ahead of their pending CTAs, or its
+    // backlog grows until launching on it blocks the submitting threads.
+    int prio_low = 0, prio_high = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->upload, cudaStreamNonBlocking, prio_high);
     s->slots.resize(c.streams);
     for (StreamSlot& sl : s->slots) {
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.s, cudaStreamNonBlocking);

@@ -108,6 +108,17 @@ def projection_ubos():
     return out
 
 
+def _pin(arrays):
+    """Page-locked copies of the arrays (torch tensors, kept by the caller), or None without CUDA."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return None
+        return [torch.from_numpy(a).pin_memory() for a in arrays]
+    except ImportError:
+        return None
+
+
 def run_load(server: Server, rate: float, duration: float, seed: int = 4, base_sets=None, p_reuse: float = 0.7,
              sigma: float = 0.1, recent_sets: int = 256, submit_threads: int = 2) -> dict:
     """cf_serve_run_load with the served mix's distributions: base light sets
@@ -117,7 +128,12 @@ def run_load(server: Server, rate: float, duration: float, seed: int = 4, base_s
         rng = np.random.default_rng(seed)
         base_sets = [scenes.blob_lights(rng, int(round(math.exp(rng.uniform(math.log(256), math.log(65536))))))
                      for _ in range(128)]
+    # pinned, as a server keeps the data it registers from: the uploads are then
+    # asynchronous copies rather than staged ones (the sets outlive the run)
     base_sets = [np.ascontiguousarray(b, np.float32) for b in base_sets]
+    pinned = _pin(base_sets)
+    if pinned is not None:
+        base_sets = [t.numpy() for t in pinned]
     projs = (CfClusterForwardUBO * 4)(*projection_ubos())
     ptrs = (C.c_void_p * len(base_sets))(*[b.ctypes.data for b in base_sets])
     counts = (C.c_uint32 * len(base_sets))(*[b.shape[0] for b in base_sets])

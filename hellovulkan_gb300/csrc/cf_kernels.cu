@@ -424,6 +424,66 @@ __device__ __forceinline__ bool scan_tile(const float4* __restrict__ tile, const
     return false;
 }
 
+// Binned: the warp's K cluster boxes stay in the item's shared-memory AABB
+// slot (wb: lo, hi per cluster; warp-uniform, read by broadcast) instead of
+// K x 6 registers per lane; only the counts and the warp's union box are
+// registers.  A capped cluster's box is set to +inf in the slot, so it never
+// hits again.  Otherwise as scan_tile with kBinned.
+template <int K>
+struct WarpCounts {
+    uint32_t cnt[K];
+    float umn[3], umx[3];
+};
+
+template <int K, bool kExact>
+__device__ __forceinline__ bool scan_tile_slot(const float4* __restrict__ tile, const uint32_t* __restrict__ idx_tile,
+                                               uint32_t n, uint32_t lane, WarpCounts<K>& w, float4* wb,
+                                               uint32_t cap, uint32_t* __restrict__ staging, uint32_t cl0,
+                                               uint32_t cl_end, uint32_t& chunks_filtered, uint32_t& chunks_tested)
+{
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    const float inf = __uint_as_float(0x7f800000u);
+    for (uint32_t j = 0; j < n; j += 32) {
+        const float4 L = tile[j + lane];
+        ++chunks_filtered;
+        if (!__any_sync(kFull, hit_fast(L, w.umn, w.umx))) continue;
+        ++chunks_tested;
+        bool h[K];
+        bool any = false;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const float4 lo = wb[2 * k], hi = wb[2 * k + 1];
+            const float mn[3] = {lo.x, lo.y, lo.z}, mx[3] = {hi.x, hi.y, hi.z};
+            h[k] = kExact ? hit_exact(L, mn, mx) : hit_fast(L, mn, mx);
+            any |= h[k];
+        }
+        if (__any_sync(kFull, any)) {
+            const uint32_t li = idx_tile[j + lane];
+            bool all_capped = true;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const uint32_t m = __ballot_sync(kFull, h[k]);
+                if (m) {
+                    const uint32_t pos = w.cnt[k] + __popc(m & lt_mask);
+                    if (h[k] && pos < cap) staging[(size_t)(cl0 + k) * cap + pos] = li;
+                    w.cnt[k] += __popc(m);
+                    if (w.cnt[k] >= cap) {
+                        w.cnt[k] = cap;
+                        if (lane == 0) {
+                            wb[2 * k] = make_float4(inf, inf, inf, 0.f);
+                            wb[2 * k + 1] = make_float4(inf, inf, inf, 0.f);
+                        }
+                        __syncwarp();
+                    }
+                }
+                all_capped = all_capped && (w.cnt[k] >= cap || cl0 + k >= cl_end);
+            }
+            if (all_capped) return true;
+        }
+    }
+    return false;
+}
+
 __device__ __forceinline__ bool tile_has_nonfinite(const uint32_t* __restrict__ flags, uint32_t base, uint32_t n)
 {
     uint32_t f = 0;
@@ -802,8 +862,8 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
         const ItemDesc& d = desc[r];  // read in place: the slot is not refilled before this item's release
         if (d.flags & kItemTerminate) break;
         const uint32_t cl0 = d.first + warp * (uint32_t)K;
-        const float4* gb = boxes + (size_t)r * kGroup * 2 + (size_t)warp * K * 2;
-        WarpClusters<K> w;
+        float4* const gb = boxes + (size_t)r * kGroup * 2 + (size_t)warp * K * 2;  // this warp's boxes
+        WarpCounts<K> w;
         bool wdone = true, union_nan = false;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
@@ -815,19 +875,26 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
             w.cnt[k] = 0;
             if (cl0 + k < d.cl_end) {
                 const float4 lo = gb[2 * k], hi = gb[2 * k + 1];
-                w.mn[k][0] = lo.x; w.mn[k][1] = lo.y; w.mn[k][2] = lo.z;
-                w.mx[k][0] = hi.x; w.mx[k][1] = hi.y; w.mx[k][2] = hi.z;
+                const float mn[3] = {lo.x, lo.y, lo.z}, mx[3] = {hi.x, hi.y, hi.z};
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
-                    union_nan |= (w.mn[k][q] != w.mn[k][q]) | (w.mx[k][q] != w.mx[k][q]);
-                    w.umn[q] = fminf(w.umn[q], w.mn[k][q]);
-                    w.umx[q] = fmaxf(w.umx[q], w.mx[k][q]);
+                    union_nan |= (mn[q] != mn[q]) | (mx[q] != mx[q]);
+                    w.umn[q] = fminf(w.umn[q], mn[q]);
+                    w.umx[q] = fmaxf(w.umx[q], mx[q]);
                 }
                 wdone = false;
-            } else {
-                for (int q = 0; q < 3; ++q) { w.mn[k][q] = inf; w.mx[k][q] = inf; }
             }
         }
+        __syncwarp();  // every lane has read the slot before lane 0 marks the absent clusters
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if (cl0 + k >= d.cl_end) {  // past the item: a box that never hits
+                    gb[2 * k] = make_float4(inf, inf, inf, 0.f);
+                    gb[2 * k + 1] = make_float4(inf, inf, inf, 0.f);
+                }
+        }
+        __syncwarp();
         if (union_nan) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
@@ -893,10 +960,10 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
             if (warp == 0 && ns + lane < nsp) surv_l[ns + lane] = make_float4(0.f, 0.f, 0.f, -inf);
             consumer_sync<WARPS * 32>();
             if (!wdone && ns) {
-                wdone = exact ? scan_tile<K, true, true>(surv_l, surv_i, nsp, 0, lane, w, d.cap, d.staging, cl0,
-                                                         d.cl_end, chunks_filtered, chunks_tested)
-                              : scan_tile<K, false, true>(surv_l, surv_i, nsp, 0, lane, w, d.cap, d.staging, cl0,
-                                                          d.cl_end, chunks_filtered, chunks_tested);
+                wdone = exact ? scan_tile_slot<K, true>(surv_l, surv_i, nsp, lane, w, gb, d.cap, d.staging, cl0,
+                                                        d.cl_end, chunks_filtered, chunks_tested)
+                              : scan_tile_slot<K, false>(surv_l, surv_i, nsp, lane, w, gb, d.cap, d.staging, cl0,
+                                                         d.cl_end, chunks_filtered, chunks_tested);
                 if (wdone && lane == 0) atomicAdd(&done[r], 1u);
             }
             consumer_sync<WARPS * 32>();  // the survivor buffer is rewritten by the next tile

@@ -783,7 +783,8 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
             const uint32_t k = item.y / gps, g = item.y % gps;
             const uint32_t first = k * xy + g * kGroup, cl_end = (k + 1) * xy;
             const uint32_t nb = min(kGroup, cl_end - first);
-            const uint32_t nsrc = v.slice_count[k];
+            const uint32_t n0 = v.slice_count[2 * k], nsrc = n0 + v.slice_count[2 * k + 1];
+            const uint32_t seg1 = list_split(v.lpad);  // where the list's second segment starts
             const uint32_t ntiles = (nsrc + TILE - 1) / TILE;
             d.staging = v.staging;
             d.counts = v.counts;
@@ -796,7 +797,7 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
             d.seq = seq;
             d.group = item.y;
             d.cap = v.cap;
-            d.flags = v.slice_nonfinite[k] ? kItemExact : 0u;
+            d.flags = (v.slice_nonfinite[2 * k] | v.slice_nonfinite[2 * k + 1]) ? kItemExact : 0u;
             done[r] = 0;
             mbar_arrive_expect_tx(smem_u32(&ifull[r]), (nb + 1) * (uint32_t)sizeof(CfAABB));
             bulk_copy_g2s(smem_u32(boxes + (size_t)r * kGroup * 2), v.aabbs + 2 * (size_t)first,
@@ -824,12 +825,23 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
                     break;
                 }
                 stop[s] = 0;
-                const uint32_t cnt = min((uint32_t)TILE, nsrc - t * TILE);
+                // list entries [pos, pos + cnt): a from the first segment, b from the second
+                const uint32_t pos = t * TILE, cnt = min((uint32_t)TILE, nsrc - pos);
+                const uint32_t a = pos < n0 ? min(cnt, n0 - pos) : 0u, b = cnt - a;
+                const uint32_t from1 = seg1 + (b ? pos + a - n0 : 0u);  // first second-segment entry
                 mbar_arrive_expect_tx(smem_u32(&full[s]), cnt * (uint32_t)(sizeof(float4) + sizeof(uint32_t)));
-                bulk_copy_g2s(smem_u32(tiles + (size_t)s * TILE), src + (size_t)t * TILE,
-                              cnt * (uint32_t)sizeof(float4), smem_u32(&full[s]));
-                bulk_copy_g2s(smem_u32(idx_tiles + (size_t)s * TILE), src_idx + (size_t)t * TILE,
-                              cnt * (uint32_t)sizeof(uint32_t), smem_u32(&full[s]));
+                if (a) {
+                    bulk_copy_g2s(smem_u32(tiles + (size_t)s * TILE), src + pos, a * (uint32_t)sizeof(float4),
+                                  smem_u32(&full[s]));
+                    bulk_copy_g2s(smem_u32(idx_tiles + (size_t)s * TILE), src_idx + pos,
+                                  a * (uint32_t)sizeof(uint32_t), smem_u32(&full[s]));
+                }
+                if (b) {
+                    bulk_copy_g2s(smem_u32(tiles + (size_t)s * TILE + a), src + from1, b * (uint32_t)sizeof(float4),
+                                  smem_u32(&full[s]));
+                    bulk_copy_g2s(smem_u32(idx_tiles + (size_t)s * TILE + a), src_idx + from1,
+                                  b * (uint32_t)sizeof(uint32_t), smem_u32(&full[s]));
+                }
             }
             seq += t;
             if (stalled) break;
@@ -1003,10 +1015,12 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
 // squares is never smaller than its z term.  NaN bounds make the slab
 // infinite; a NaN coordinate contributes 0 and is kept; slices holding a
 // light with a non-finite coordinate are flagged for the exact test.
-// One CTA of WARPS warps bins SLICES consecutive slices: every light it reads
-// is tested against each of their slabs, so the view-space lights are read
-// once per SLICES slices (a batch bins 4 slices per 512-thread CTA; a single
-// view, which has few slices, one slice per 1024-thread CTA).  Each step bins
+// One CTA of WARPS warps bins one segment of SLICES consecutive slices: every
+// light it reads is tested against each of their slabs, so the view-space
+// lights are read once per SLICES slices (a batch bins 4 slices per
+// 512-thread CTA into their lists' first segments; a single view, which has
+// few slices, one slice per 1024-thread CTA and two CTAs per slice, one per
+// segment, so that it keeps twice as many SMs busy).  Each step bins
 // WARPS x 128 lights (4 chunks of 32 per warp) with ballot/popc and, per
 // slice, a warp scan of the warps' counts.  Every thread stages its own four
 // lights of the next step in shared memory with cp.async while it bins the
@@ -1020,9 +1034,10 @@ constexpr int kBinWarpsBatch = 16, kBinSlicesBatch = 4;
 // dynamic shared memory of a binning CTA: two slots of kBinChunks lights per thread
 constexpr size_t bin_stage_bytes(int warps) { return 2ull * kBinChunks * (size_t)warps * 32 * sizeof(float4); }
 
-template <int kBinWarps, int kBinSlicesT>
+template <int kBinWarps, int kBinSlicesT, int kParts>
 __device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
 {
+    static_assert(kParts == 1 || kParts == 2, "a list has two segments");
     constexpr uint32_t kBinSlices = (uint32_t)kBinSlicesT;
     __shared__ float s_lo[kBinSlices][kBinWarps], s_hi[kBinSlices][kBinWarps];
     __shared__ uint32_t s_cnt[kBinSlices][kBinWarps];
@@ -1031,23 +1046,26 @@ __device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
     constexpr uint32_t kThreads = kBinWarps * 32;
     constexpr uint32_t kStep = kBinWarps * kBinChunks * 32;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t xy = v.slice_clusters, k0 = blk * kBinSlices;
+    const uint32_t h = kParts == 2 ? (blk & 1u) : 0u;  // the list segment this CTA writes
+    const uint32_t xy = v.slice_clusters, k0 = (kParts == 2 ? blk >> 1 : blk) * kBinSlices;
     const uint32_t ns = min(kBinSlices, v.slices - k0);
+    const uint32_t seg_lo = h ? list_split(v.lpad) : 0u;                       // lights [seg_lo, seg_hi)
+    const uint32_t seg_hi = kParts == 2 && h == 0 ? list_split(v.lpad) : v.lpad;
     const float inf = __uint_as_float(0x7f800000u);
     // this thread's lights of the step at `base` into slot `slot`
     auto stage = [&](uint32_t base, uint32_t slot) {
 #pragma unroll
         for (int q = 0; q < kBinChunks; ++q) {
             const uint32_t i = base + warp * (kBinChunks * 32) + q * 32 + lane;
-            if (i < v.lpad) cp_async16(smem_u32(&bin_stage[(slot * kBinChunks + q) * kThreads + tid]), &v.vlights[i]);
+            if (i < seg_hi) cp_async16(smem_u32(&bin_stage[(slot * kBinChunks + q) * kThreads + tid]), &v.vlights[i]);
         }
         cp_async_commit();
     };
-    stage(0, 0);  // in flight during the slab reduction
+    stage(seg_lo, 0);  // in flight during the slab reduction
     if (tid == 0) {
         s_nan = 0;
         s_nonfinite = 0;
-        if (k0 == 0 && v.queue) *v.queue = 0u;  // the single-view culling launch's item counter
+        if (k0 == 0 && h == 0 && v.queue) *v.queue = 0u;  // the single-view culling launch's item counter
     }
     __syncthreads();
     // One pass over each slice's cluster AABBs: the slab (lowest min.z,
@@ -1057,7 +1075,8 @@ __device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
     // with xor shuffles.  A NaN bound makes the slab, or the group's box,
     // infinite.
     const uint32_t gw = v.group_width, gps = (xy + gw - 1) / gw;
-    const uint32_t span = v.group_boxes ? gps * gw : xy;  // clusters a pass covers (groups padded)
+    const bool write_boxes = v.group_boxes && h == 0;  // the first segment's CTA writes the group boxes
+    const uint32_t span = write_boxes ? gps * gw : xy;  // clusters a pass covers (groups padded)
 #pragma unroll
     for (uint32_t sl = 0; sl < kBinSlices; ++sl) {
         float lo = inf, hi = -inf;
@@ -1074,7 +1093,7 @@ __device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
                     lo = fminf(lo, a.z);
                     hi = fmaxf(hi, b.z);
                 }
-                if (v.group_boxes) {
+                if (write_boxes) {
                     bool gnan = (a.x != a.x) | (a.y != a.y) | (a.z != a.z) | (b.x != b.x) | (b.y != b.y) | (b.z != b.z);
                     for (uint32_t o = 1; o < gw; o <<= 1) {
                         a.x = fminf(a.x, __shfl_xor_sync(kFull, a.x, o));
@@ -1125,9 +1144,9 @@ __device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
     uint32_t running[kBinSlices] = {};
     uint32_t nonfinite = 0;  // bit sl: this thread binned a non-finite light into slice sl
     uint32_t slot = 0;
-    for (uint32_t base = 0; base < v.lpad; base += kStep, slot ^= 1u) {
+    for (uint32_t base = seg_lo; base < seg_hi; base += kStep, slot ^= 1u) {
         // the other slot was read into registers a step ago, before a barrier
-        if (base + kStep < v.lpad) {
+        if (base + kStep < seg_hi) {
             stage(base + kStep, slot ^ 1u);
             cp_async_wait<1>();
         } else {
@@ -1138,7 +1157,7 @@ __device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
 #pragma unroll
         for (int q = 0; q < kBinChunks; ++q) {
             const uint32_t i = base + warp * (kBinChunks * 32) + q * 32 + lane;
-            L[q] = i < v.lpad ? bin_stage[(slot * kBinChunks + q) * kThreads + tid] : make_float4(0.f, 0.f, 0.f, -inf);
+            L[q] = i < seg_hi ? bin_stage[(slot * kBinChunks + q) * kThreads + tid] : make_float4(0.f, 0.f, 0.f, -inf);
             fin[q] = finite_bits(L[q].x) && finite_bits(L[q].y) && finite_bits(L[q].z);
         }
         uint32_t m[kBinSlices][kBinChunks];
@@ -1162,8 +1181,8 @@ __device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
             const uint32_t c = lane < kBinWarps ? s_cnt[sl][lane] : 0u;
             const uint32_t incl = warp_inclusive_scan(c, lane);
             uint32_t pos = running[sl] + __shfl_sync(kFull, incl - c, warp);
-            float4* out_l = v.slice_lights + (size_t)(k0 + sl) * v.lpad;
-            uint32_t* out_i = v.slice_idx + (size_t)(k0 + sl) * v.lpad;
+            float4* out_l = v.slice_lights + (size_t)(k0 + sl) * v.lpad + seg_lo;
+            uint32_t* out_i = v.slice_idx + (size_t)(k0 + sl) * v.lpad + seg_lo;
 #pragma unroll
             for (int q = 0; q < kBinChunks; ++q) {
                 if ((m[sl][q] >> lane) & 1u) {
@@ -1181,25 +1200,31 @@ __device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
 #pragma unroll
     for (uint32_t sl = 0; sl < kBinSlices; ++sl) {
         if (sl >= ns) break;
-        const uint32_t npad = (running[sl] + 31) & ~31u;
-        float4* out_l = v.slice_lights + (size_t)(k0 + sl) * v.lpad;
-        uint32_t* out_i = v.slice_idx + (size_t)(k0 + sl) * v.lpad;
+        const uint32_t npad = (running[sl] + 31) & ~31u;  // <= seg_hi - seg_lo: both are multiples of 32
+        float4* out_l = v.slice_lights + (size_t)(k0 + sl) * v.lpad + seg_lo;
+        uint32_t* out_i = v.slice_idx + (size_t)(k0 + sl) * v.lpad + seg_lo;
         for (uint32_t p = running[sl] + tid; p < npad; p += kBinWarps * 32) {
             out_l[p] = make_float4(0.f, 0.f, 0.f, -inf);
             out_i[p] = 0;
         }
-        if (tid == 0) v.slice_count[k0 + sl] = npad;
+        if (tid == 0) {
+            v.slice_count[2 * (k0 + sl) + h] = npad;
+            if (kParts == 1) v.slice_count[2 * (k0 + sl) + 1] = 0u;  // an empty second segment
+        }
     }
     __syncthreads();
-    if (tid < ns) v.slice_nonfinite[k0 + tid] = (s_nonfinite >> tid) & 1u;
-    if (tid == 0 && v.work) atomicAdd(&v.work[0], (unsigned long long)v.lpad * ns);
+    if (tid < ns) {
+        v.slice_nonfinite[2 * (k0 + tid) + h] = (s_nonfinite >> tid) & 1u;
+        if (kParts == 1) v.slice_nonfinite[2 * (k0 + tid) + 1] = 0u;
+    }
+    if (tid == 0 && v.work) atomicAdd(&v.work[0], (unsigned long long)(seg_hi - seg_lo) * ns);
 }
 
 __global__ void __launch_bounds__(kBinWarpsSingle * 32) bin_slices_kernel(const ViewCull v)
 {
     grid_dependency_wait();
     launch_dependents();
-    bin_slices_body<kBinWarpsSingle, kBinSlicesSingle>(v, blockIdx.x);
+    bin_slices_body<kBinWarpsSingle, kBinSlicesSingle, 2>(v, blockIdx.x);
 }
 
 // Batched binning: block b is slice block b - prefix[v] of view v.
@@ -1212,7 +1237,7 @@ __global__ void __launch_bounds__(kBinWarpsBatch * 32, 2) batch_bin_kernel(const
     // that their long blocks start in the first wave
     const uint32_t r = find_view(prefix, n_views, blockIdx.x);
     const uint32_t vi = order ? __ldg(&order[r]) : r;
-    bin_slices_body<kBinWarpsBatch, kBinSlicesBatch>(jobs[vi].v, blockIdx.x - __ldg(&prefix[r]));
+    bin_slices_body<kBinWarpsBatch, kBinSlicesBatch, 1>(jobs[vi].v, blockIdx.x - __ldg(&prefix[r]));
 }
 
 // ---------------------------------------------------------------------------
@@ -1535,9 +1560,9 @@ WorkspaceLayout workspace_layout(uint32_t clusters, uint32_t lights, uint32_t ca
         w.slice_idx = off;
         off += al((size_t)slices * lpad * sizeof(uint32_t));
         w.slice_count = off;
-        off += al((size_t)slices * sizeof(uint32_t));
+        off += al((size_t)2 * slices * sizeof(uint32_t));
         w.slice_nonfinite = off;
-        off += al((size_t)slices * sizeof(uint32_t));
+        off += al((size_t)2 * slices * sizeof(uint32_t));
         w.group_boxes = off;
         off += al((size_t)groups * 2 * sizeof(float4));
     }
@@ -1571,7 +1596,7 @@ cudaError_t launch_bin(const ViewCull& v, cudaStream_t stream)
     static const cudaError_t attr =  // one-time opt-in above 48 KB
         cudaFuncSetAttribute(bin_slices_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (attr != cudaSuccess) return attr;
-    return launch_kernel(true, bin_slices_kernel, dim3((v.slices + kBinSlicesSingle - 1) / kBinSlicesSingle),
+    return launch_kernel(true, bin_slices_kernel, dim3((v.slices + kBinSlicesSingle - 1) / kBinSlicesSingle * 2),
                              dim3(kBinWarpsSingle * 32), smem, stream, v);
 }
 

@@ -35,6 +35,9 @@ constexpr uint32_t kErrEmptyWaitTimeout = 1u << 1;  // the producer waited too l
 
 inline uint32_t pad_lights(uint32_t n) { return (n + kLightPad - 1) / kLightPad * kLightPad; }
 inline uint32_t granules(uint32_t lpad) { return (lpad + kFlagGranule - 1) / kFlagGranule; }
+// Start of a slice list's second segment (see ViewCull): half the padded
+// lights, rounded up to a multiple of 32.
+__host__ __device__ inline uint32_t list_split(uint32_t lpad) { return (lpad / 32 + 1) / 2 * 32; }
 
 struct ViewCull {
     const float4* vlights;
@@ -48,8 +51,13 @@ struct ViewCull {
     // binned path: per depth slice, a candidate list of lpad entries
     float4* slice_lights;
     uint32_t* slice_idx;
-    uint32_t* slice_count;      // padded length of each slice's list
-    uint32_t* slice_nonfinite;  // 1 when a listed light has a non-finite coordinate
+    // A slice's list is two segments, each in ascending light order and
+    // padded to a multiple of 32: the candidates among lights [0, S) at the
+    // list's start, those among [S, lpad) from entry S (S = list_split(lpad));
+    // the list is the first followed by the second.  A single view bins the
+    // two with separate CTAs; a batch writes everything to the first.
+    uint32_t* slice_count;      // [2k + h]: padded length of segment h of slice k
+    uint32_t* slice_nonfinite;  // [2k + h]: 1 when segment h lists a light with a non-finite coordinate
     float4* group_boxes;        // per cluster group, the union of its AABBs (lo, hi; NaN bound: infinite)
     // optional work counters (profiling only, null otherwise): [0] sphere-box
     // tests against slice slabs and warp union boxes, [1] sphere-box tests

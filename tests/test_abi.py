@@ -75,7 +75,7 @@ def test_status_strings_and_argument_errors_without_gpu(cflib):
     # candidate lists (float4 + index), slice counts, slice flags and the
     # groups' union boxes
     assert n.value == (256 + al(16384 * 16) + al(64 * 4) + al(27648 * 4) + al(27648 * 150 * 4) + 2 * al(1728 * 4)
-                       + al(48 * 16384 * 16) + al(48 * 16384 * 4) + 2 * al(48 * 4) + al(1728 * 32))
+                       + al(48 * 16384 * 16) + al(48 * 16384 * 4) + 2 * al(2 * 48 * 4) + al(1728 * 32))
     ubo = _lib.CfClusterForwardUBO()
     ubo.sliceCountX, ubo.sliceCountY, ubo.sliceCountZ = 0, 9, 24
     assert L.cf_generate_aabbs(C.byref(ubo), C.c_void_p(256), None) == 1

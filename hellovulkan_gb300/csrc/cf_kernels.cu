@@ -1222,6 +1222,17 @@ __device__ __forceinline__ void bin_slices_body(const ViewCull& v, uint32_t blk)
 
 __global__ void __launch_bounds__(kBinWarpsSingle * 32) bin_slices_kernel(const ViewCull v)
 {
+    // The slice's cluster AABBs do not come from the light transform this
+    // launch waits for: pull them into L2 while it finishes (a hint only; the
+    // loads below still read them after the wait).
+    {
+        const uint32_t k = (blockIdx.x >> 1) * kBinSlicesSingle;
+        const uint32_t ns = min((uint32_t)kBinSlicesSingle, v.slices - k);
+        const char* p = reinterpret_cast<const char*>(v.aabbs + 2 * (size_t)k * v.slice_clusters);
+        const uint32_t lines = (ns * v.slice_clusters * (uint32_t)sizeof(CfAABB) + 127) / 128;
+        for (uint32_t l = threadIdx.x; l < lines; l += blockDim.x)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(p + 128 * (size_t)l));
+    }
     grid_dependency_wait();
     launch_dependents();
     bin_slices_body<kBinWarpsSingle, kBinSlicesSingle, 2>(v, blockIdx.x);
@@ -1375,16 +1386,17 @@ __global__ void __launch_bounds__(kCopyThreads) copy_kernel(const ViewCull v)
     const uint32_t b = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
     uint32_t first, end;
     group_range(v, b, &first, &end);
+    const uint32_t c = first + lane;
+    const uint32_t cnt = tid < 32 && c < end ? v.counts[c] : 0u;  // in flight during the sum below
     if constexpr (kSumGroups) {
         uint32_t part = 0;
+#pragma unroll 4
         for (uint32_t j = tid; j < b; j += kCopyThreads) part += __ldg(&v.group_sums[j]);
         part = warp_sum(part);
         if (lane == 0) s_part[tid >> 5] = part;
         __syncthreads();
     }
     if (tid < 32) {
-        const uint32_t c = first + lane;
-        const uint32_t cnt = c < end ? v.counts[c] : 0u;
         const uint32_t incl = warp_inclusive_scan(cnt, lane);
         uint32_t base;
         if constexpr (kSumGroups) base = warp_sum(lane < kCopyThreads / 32 ? s_part[lane] : 0u);

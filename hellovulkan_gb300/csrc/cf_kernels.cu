@@ -771,7 +771,9 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
                 break;
             }
             ItemDesc& d = desc[r];
-            const uint32_t it = *s_abort ? n_items : atomicAdd(queue, 1u);
+            // each CTA's first item is its own index, the rest come from the
+            // counter (one atomic round trip less before the first item)
+            const uint32_t it = *s_abort ? n_items : n == 0 ? blockIdx.x : gridDim.x + atomicAdd(queue, 1u);
             if (it >= n_items) {
                 d.flags = kItemTerminate;
                 mbar_arrive(smem_u32(&ifull[r]));

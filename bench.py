@@ -392,8 +392,8 @@ def measure_serve(ctx, seconds, rates=(2000.0, 10000.0, 50000.0), sweep=(20000.0
     def stall_ms(r):
         # the longest single CUDA call inside the register / jitter / submit
         # entry points: a host-side copy or launch normally returns in tens of
-        # microseconds, so one that blocked for over 10 ms means the driver
-        # stopped taking work from every thread at once
+        # microseconds, so one that blocked for over 10 ms means the CUDA
+        # driver stopped taking work from every thread of the process at once
         return max(r["register_call_max_us"], r["jitter_call_max_us"], r["submit_call_max_us"]) / 1e3
 
     def measured(rate, dur):

@@ -72,6 +72,21 @@ def test_dense_slices_with_a_short_last_group(gpu, oracle, tuning):
     assert_matches_oracle(oracle, v, *run_pipeline(gpu, v, tuning))
 
 
+@pytest.mark.parametrize("n_lights", [1, 31, 33, 64, 65, 4097, 8193])
+def test_list_segments_around_the_split(gpu, oracle, n_lights):
+    """A binned single view bins each slice with two CTAs, one per half of
+    the padded lights, into two segments of the slice's list: light counts
+    around the split point, an empty second segment, tiles that take lights
+    from both segments, and a non-finite light that only the second segment
+    lists (its slices take the exact test)."""
+    rng = np.random.default_rng(31 + n_lights)
+    lights = scenes.uniform_box_lights(rng, n_lights, [-30, -15, -60], [30, 15, -5], 2.0, 6.0)
+    if n_lights >= 33:
+        lights[n_lights - 1, 1] = np.inf
+    v = scenes.custom_view((15, 9, 24), 1920, 1080, 0.1, 300.0, lights=lights)
+    assert_matches_oracle(oracle, v, *run_pipeline(gpu, v, (2, 8, 1024, 2, 1)))
+
+
 @pytest.mark.parametrize("tuning", [(1, 4, 512, 4, 0), (1, 4, 256, 4, 1), (2, 8, 1024, 2, 1)])
 def test_offsets_with_and_without_a_scan_launch(gpu, oracle, tuning):
     """Views of more than 8192 cluster groups scan the group totals in a launch

@@ -5,7 +5,9 @@
 //   light_xform_kernel  the `ubo.cameraView * posWorld` and `radius * radius` of
 //   batch_xform_kernel  LightCulling.comp:51-56, hoisted to once per light
 //   bin_slices_kernel   per depth slice, the lights whose sphere can reach the
-//   batch_bin_kernel    slice's z slab, in light order (the candidate lists)
+//   batch_bin_kernel    slice's z slab, in light order (the candidate lists; a
+//                       single view's in two segments, one CTA per half of the
+//                       lights)
 //   cull_kernel         LightCulling.comp:59-77 brute force: a producer warp
 //                       streams tiles of view-space lights into shared memory
 //                       with bulk async copies (cp.async.bulk + mbarrier); each

@@ -357,6 +357,34 @@ def measure_batch(ctx, stream, n_views=256, passes=20, seed=3, sample_views=6):
     }
 
 
+HOST_STALL_MS = 10.0
+
+
+def host_stall_ms(run) -> float:
+    """The longest single CUDA call inside a served run's register / jitter /
+    submit entry points, in ms.  A host-side copy or launch normally returns
+    in tens of microseconds, so one that blocked for over HOST_STALL_MS means
+    the CUDA driver stopped taking work from every thread of the process at
+    once."""
+    return max(run["register_call_max_us"], run["jitter_call_max_us"], run["submit_call_max_us"]) / 1e3
+
+
+def measured_once_more_after_stall(run_fn):
+    """One served run (run_fn() -> dict with "sustained" and the call maxima).
+    A run that misses the bound while one of its CUDA calls blocked for over
+    HOST_STALL_MS is recorded under "stalled_run" of a second run, which is
+    the one reported, as a clock-throttled run would be measured again; any
+    other run is reported as it is."""
+    x = run_fn()
+    x["host_stall_ms"] = host_stall_ms(x)
+    if not x["sustained"] and x["host_stall_ms"] > HOST_STALL_MS:
+        y = run_fn()
+        y["host_stall_ms"] = host_stall_ms(y)
+        y["stalled_run"] = {k: x[k] for k in ("latency_p99_ms", "latency_max_ms", "host_stall_ms", "achieved_rate")}
+        x = y
+    return x
+
+
 def measure_serve(ctx, seconds, rates=(2000.0, 10000.0, 50000.0), sweep=(20000.0, 40000.0, 60000.0, 80000.0,
                                                                         100000.0, 120000.0, 150000.0, 200000.0),
                   sweep_seconds=5.0, submit_threads=4):
@@ -389,25 +417,8 @@ def measure_serve(ctx, seconds, rates=(2000.0, 10000.0, 50000.0), sweep=(20000.0
                   rep["achieved_rate"] >= 0.98 * rep["offered_rate"]})
         return r
 
-    def stall_ms(r):
-        # the longest single CUDA call inside the register / jitter / submit
-        # entry points: a host-side copy or launch normally returns in tens of
-        # microseconds, so one that blocked for over 10 ms means the CUDA
-        # driver stopped taking work from every thread of the process at once
-        return max(r["register_call_max_us"], r["jitter_call_max_us"], r["submit_call_max_us"]) / 1e3
-
     def measured(rate, dur):
-        # a run that misses the bound during such a stall is recorded with its
-        # stall and measured once more, as a clock-throttled run would be
-        x = one(rate, dur, submit_threads)
-        x["host_stall_ms"] = stall_ms(x)
-        if not x["sustained"] and x["host_stall_ms"] > 10.0:
-            y = one(rate, dur, submit_threads)
-            y["host_stall_ms"] = stall_ms(y)
-            y["stalled_run"] = {k: x[k] for k in ("latency_p99_ms", "latency_max_ms", "host_stall_ms",
-                                                  "achieved_rate")}
-            x = y
-        return x
+        return measured_once_more_after_stall(lambda: one(rate, dur, submit_threads))
 
     runs = [measured(r, seconds) for r in rates]
     swept, best = [], 0.0

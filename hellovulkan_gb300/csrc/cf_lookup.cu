@@ -197,7 +197,10 @@ __device__ __forceinline__ void radiance(const CfLightData* __restrict__ light, 
         const float spec = cf_fdiv(cf_fmul(DG, fc[c]), denom);
         const float kd = cf_fmul(cf_fsub(1.0f, fc[c]), km);
         const float diff = cf_fdiv(cf_fmul(kd, ac[c]), kPi);
-        out[c] = cf_fmul(cf_fmul(cf_fadd(diff, spec), rc[c]), NoL);
+        // Radiance's own Lo starts at vec3(0.0) (Radiance.glsl:13,55): the
+        // term is added to zero before Scene.frag adds it to its Lo, which
+        // turns a -0 term into +0
+        out[c] = cf_fadd(0.0f, cf_fmul(cf_fmul(cf_fadd(diff, spec), rc[c]), NoL));
     }
     lo = V3{cf_fadd(lo.x, out[0]), cf_fadd(lo.y, out[1]), cf_fadd(lo.z, out[2])};
 }

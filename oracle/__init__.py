@@ -5,9 +5,11 @@ and by the CPU-baseline leg of ``bench.py``, as the checker of the CUDA path.
 
 * ``Oracle`` wraps ``oracle/_build/libcf_oracle.so`` (cf_oracle.cpp, the
   restatement of AABBGenerator.comp and LightCulling.comp).
-* ``Reference`` wraps ``oracle/_ref/libcf_ref.so``: the reference's own two
-  shaders compiled as C++ (see oracle/build.py); available only where their
-  generated translation unit exists.
+* ``Reference`` wraps ``oracle/_ref/libcf_ref.so``: the reference's own
+  shaders compiled as C++ (AABBGenerator.comp, LightCulling.comp,
+  FrustumCulling.comp and Scene.frag's lookup and direct lighting; see
+  oracle/build.py); available only where their generated translation unit
+  exists.
 """
 from __future__ import annotations
 
@@ -135,13 +137,19 @@ class Oracle:
 
 
 class Reference:
-    """The reference's AABBGenerator.comp / LightCulling.comp run on the CPU."""
+    """The reference's shaders run on the CPU: AABBGenerator.comp,
+    LightCulling.comp, FrustumCulling.comp, and Scene.frag's clustered lookup
+    and direct lighting."""
 
     def __init__(self, path: Path):
         L = C.CDLL(str(path))
         L.cfr_generate_aabbs.argtypes = [_P, _P, C.c_int]
         L.cfr_cull.argtypes = [_P, _P, _P, C.c_uint32, _P, _P, C.c_uint64, C.POINTER(C.c_uint32), C.c_int]
         L.cfr_max_lights_per_cluster.restype = C.c_uint32
+        L.cfr_frustum_cull.argtypes = [_P, _P, C.c_uint32, _P, C.c_int]
+        L.cfr_lookup_fragments.argtypes = [_P, _P, C.c_uint32, C.c_uint32, _P, C.c_uint32, _P, _P, _P, _P, C.c_int]
+        L.cfr_shade_fragments.argtypes = [_P, _P, _P, _P, C.c_uint32, C.c_uint32, _P, C.c_uint32, _P, C.c_uint64, _P,
+                                          C.c_uint32, _P, _P, C.c_int]
         self.lib = L
         self.cap = int(L.cfr_max_lights_per_cluster())
 
@@ -174,6 +182,49 @@ class Reference:
                                lights.shape[0], cells.ctypes.data, idx.ctypes.data, cap_total, C.byref(total), threads)
         assert st == 0, st
         return cells, idx[: total.value].copy()
+
+    def frustum_cull(self, frustum, boxes: np.ndarray, threads: int = 1) -> np.ndarray:
+        """FrustumCulling.comp's instanceCount (0 or 1) for each box."""
+        b = np.ascontiguousarray(boxes, np.float32).reshape(-1, 8)
+        out = np.zeros(b.shape[0], np.uint32)
+        st = self.lib.cfr_frustum_cull(C.byref(frustum), b.ctypes.data if b.size else None, b.shape[0],
+                                       out.ctypes.data if out.size else None, threads)
+        assert st == 0, st
+        return out
+
+    def lookup_fragments(self, ubo, depth: np.ndarray, cells: np.ndarray, threads: int = 1):
+        """Scene.frag's clustered lookup per pixel: dict of cluster, count,
+        offset (uint32) and linear_depth (float32), each shaped like depth.
+        A fragment past the grid reads a zero cell (robust buffer access)."""
+        depth = np.ascontiguousarray(depth, np.float32)
+        h, w = depth.shape
+        cells = np.ascontiguousarray(cells, np.uint32).reshape(-1, 2)
+        out = {k: np.zeros(depth.shape, np.uint32) for k in ("cluster", "count", "offset")}
+        out["linear_depth"] = np.zeros(depth.shape, np.float32)
+        st = self.lib.cfr_lookup_fragments(_ubo_ptr(ubo), depth.ctypes.data, w, h, cells.ctypes.data, cells.shape[0],
+                                           out["cluster"].ctypes.data, out["count"].ctypes.data,
+                                           out["offset"].ctypes.data, out["linear_depth"].ctypes.data, threads)
+        assert st == 0, st
+        return out
+
+    def shade_fragments(self, ubo, camera_position, pc, gbuffer: np.ndarray, cells: np.ndarray, indices: np.ndarray,
+                        lights: np.ndarray, threads: int = 1):
+        """Scene.frag's direct clustered lighting per G-buffer texel: (Lo as
+        (h, w, 3) float32, the looked-up cluster index as (h, w) uint32)."""
+        g = np.ascontiguousarray(gbuffer, np.float32)
+        h, w = g.shape[:2]
+        cells = np.ascontiguousarray(cells, np.uint32).reshape(-1, 2)
+        indices = np.ascontiguousarray(indices, np.uint32)
+        lights = np.ascontiguousarray(lights, np.float32).reshape(-1, 12)
+        cam = (C.c_float * 3)(*[float(v) for v in camera_position[:3]])
+        rgb = np.zeros((h, w, 3), np.float32)
+        cl = np.zeros((h, w), np.uint32)
+        st = self.lib.cfr_shade_fragments(_ubo_ptr(ubo), cam, C.byref(pc), g.ctypes.data, w, h, cells.ctypes.data,
+                                          cells.shape[0], indices.ctypes.data if indices.size else None, indices.size,
+                                          lights.ctypes.data if lights.size else None, lights.shape[0],
+                                          rgb.ctypes.data, cl.ctypes.data, threads)
+        assert st == 0, st
+        return rgb, cl
 
 
 def jitter_lights(lights: np.ndarray, seed: int, sigma: float) -> np.ndarray:

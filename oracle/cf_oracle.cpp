@@ -356,7 +356,9 @@ int cfo_shade_clusters(const CfClusterForwardUBO* ubo, const float* cam, const C
                         const float kd = (1.0f - F) * (1.0f - metallic);
                         const float diff = kd * A[c] / pi;
                         const float rad = L.color[c] * att * pc->lightIntensity;
-                        lo[c] = lo[c] + (diff + spec) * rad * NoL;
+                        // Radiance returns its own Lo, vec3(0.0) plus the term
+                        // (Radiance.glsl:13,55): 0 + (-0) is +0
+                        lo[c] = lo[c] + (0.0f + (diff + spec) * rad * NoL);
                     }
                 }
             }

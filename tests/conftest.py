@@ -43,6 +43,14 @@ def golden():
 
 
 @pytest.fixture(scope="session")
+def golden_consumers():
+    """FrustumCulling.comp and Scene.frag's lookup and lighting outputs made
+    by the reference's own shader code (tests/golden/make_golden.py)."""
+    import numpy as np
+    return np.load(REPO / "tests" / "golden" / "golden_consumers.npz")
+
+
+@pytest.fixture(scope="session")
 def gpu(cflib):
     import torch
     if not torch.cuda.is_available():

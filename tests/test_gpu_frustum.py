@@ -1,5 +1,6 @@
 """GPU tests of FrustumCulling.comp (cf_frustum_cull): every box's
-instanceCount bit for bit against the oracle, the commands' other fields
+instanceCount bit for bit against the oracle and against the reference
+shader's own outputs (golden_consumers.npz), the commands' other fields
 untouched, and the optional visible count."""
 import math
 
@@ -43,3 +44,20 @@ def test_frustum_culling_matches_the_oracle(gpu, oracle, n, seed):
         assert np.array_equal(got[:, 1], want)
         assert np.array_equal(got[:, [0, 2, 3]], cmds[:, [0, 2, 3]])
         assert int(visible.item()) == int(want.sum()) and 0 < want.sum() < n
+
+
+def test_frustum_culling_matches_the_reference_golden(gpu, golden_consumers):
+    """The fixture's boxes (random, inverted, degenerate, huge, infinite, NaN,
+    signed-zero) under three frusta: the kernel's single-corner plane test
+    gives FrustumCulling.comp's eight-corner answers."""
+    import torch
+    from hellovulkan_gb300._lib import CfFrustum
+    from hellovulkan_gb300.consumer import frustum_cull
+    boxes = golden_consumers["frustum/boxes"]
+    d_boxes = torch.from_numpy(boxes).cuda()
+    for k in range(3):
+        f = CfFrustum.from_buffer_copy(golden_consumers["frustum/f%d" % k].tobytes())
+        d_cmds = torch.zeros((boxes.shape[0], 4), dtype=torch.int32, device="cuda")
+        frustum_cull(f, d_boxes, d_cmds)
+        got = d_cmds.cpu().numpy().view(np.uint32)[:, 1]
+        assert np.array_equal(got, golden_consumers["frustum/instance%d" % k].astype(np.uint32)), k

@@ -1,6 +1,7 @@
 """GPU tests of Scene.frag's cluster lookup over the culled lists
 (cf_lookup_clusters): every per-pixel field bit for bit against the oracle,
-and the drop-in property at full resolution (a light that contains a
+the cluster, cell and LinearDepth against the reference fragment code's own
+outputs (golden_consumers.npz), and the drop-in property at full resolution (a light that contains a
 fragment is in its cluster's list unless the fragment lies outside the
 cluster's box or the list is capped)."""
 import numpy as np
@@ -63,3 +64,22 @@ def test_lookup_drop_in_property_at_full_resolution(gpu):
     assert not np.any((s["missing"] > 0) & ~explained)
     assert explained.mean() < 1e-3  # boundary rounding only
     assert np.all(s["covering"] <= s["count"])
+
+
+def test_lookup_matches_the_reference_golden(gpu, golden_consumers):
+    """cluster, count, offset and LinearDepth bits as Scene.frag:54-78 computes
+    them (a fragment past the last slice reads a zero cell there, and is
+    flagged OUTSIDE_GRID with count 0 here)."""
+    from hellovulkan_gb300.camera import ubo_from_bytes
+    g = golden_consumers
+    ubo = ubo_from_bytes(g["frag/ubo"])
+    cells, idx = g["frag/cells"], g["frag/indices"]
+    v = scenes.View(ubo, g["frag/lights"], 150, "golden")
+    aabbs = np.zeros((cells.shape[0], 8), np.float32)
+    s = device_lookup(v, g["frag/depth"], cells, idx, aabbs, check_all=False)
+    inside = g["frag/lookup_cluster"] < cells.shape[0]
+    assert np.array_equal((s["flags"] & FRAGMENT_OUTSIDE_GRID) == 0, inside)
+    assert np.array_equal(s["cluster"][inside], g["frag/lookup_cluster"][inside])
+    assert np.array_equal(s["count"], g["frag/lookup_count"])
+    assert np.array_equal(s["offset"], g["frag/lookup_offset"])
+    assert np.array_equal(s["linear_depth"].view(np.uint32), g["frag/lookup_linear_depth"])

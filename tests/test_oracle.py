@@ -1,5 +1,7 @@
 """CPU tests of the oracle: pinned math, agreement with the reference's own
-shaders compiled as C++, the committed golden fixtures and hand-made cases."""
+shaders compiled as C++ (the two culling passes, frustum culling, and
+Scene.frag's lookup and direct lighting), the committed golden fixtures and
+hand-made cases."""
 import hashlib
 import math
 
@@ -205,3 +207,138 @@ def test_oracle_frustum_culling_keeps_what_the_camera_sees():
         return b
     boxes = np.stack([box((0, 0, -10)), box((0, 0, 10)), box((0, 0, -200)), box((50, 0, -10)), box((0, 0, -99.9))])
     assert o.frustum_cull(f, boxes).tolist() == [1, 0, 0, 0, 1]
+
+
+# --- consumer passes: oracle == the reference's shader code --------------------
+
+PC_DEFAULT = (1.75, 0.01, 0.0, 0.1, 0.1)  # the reference UI's defaults (Header/UIData.h:23-29)
+
+
+def edge_boxes(rng, n):
+    """Random boxes, then inverted, degenerate, huge, infinite, NaN and
+    signed-zero ones: the cases where the GPU's single-corner plane test must
+    fall back to the shader's eight-corner count."""
+    b = scenes.random_boxes(rng, n)
+    k = n // 16
+    b[:k, [0, 4]] = b[:k, [4, 0]]
+    b[k:2 * k, 4:7] = b[k:2 * k, 0:3]
+    b[2 * k:2 * k + 32, 0] = -3e20
+    b[2 * k + 32:2 * k + 64, 5] = np.inf
+    b[2 * k + 64:2 * k + 96, 2] = np.nan
+    b[2 * k + 96:2 * k + 128, 0:3] = -0.0
+    b[2 * k + 96:2 * k + 128, 4:7] = 0.0
+    b[2 * k + 128:2 * k + 160, 0:3] = -1e30
+    b[2 * k + 128:2 * k + 160, 4:7] = 1e30
+    return b
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_oracle_frustum_matches_reference_shader(oracle, reference, seed):
+    """cfo_frustum_cull == FrustumCulling.comp:14-57 compiled as C++."""
+    from hellovulkan_gb300.camera import frustum_ubo
+    rng = np.random.default_rng(seed)
+    boxes = edge_boxes(rng, 20000)
+    for _ in range(3):
+        f = frustum_ubo(math.radians(rng.uniform(30, 90)), rng.uniform(1.0, 2.5), 0.1, float(rng.uniform(100, 1000)),
+                        scenes.random_camera(rng))
+        want = reference.frustum_cull(f, boxes, threads=4)
+        assert np.array_equal(oracle.frustum_cull(f, boxes), want)
+        assert 0 < want.sum() < boxes.shape[0]
+
+
+def _fragment_views():
+    rng = np.random.default_rng(31)
+    return [scenes.custom_view((16, 9, 24), 320, 180, 0.1, 1000.0, scenes.random_camera(rng),
+                               scenes.blob_lights(rng, 2000)),
+            scenes.custom_view((7, 5, 3), 140, 100, 0.2, 80.0, np.eye(4, dtype=np.float32),
+                               scenes.uniform_box_lights(rng, 333, [-30, -20, -90], [30, 20, 10], 0.5, 6.0))]
+
+
+@pytest.mark.parametrize("case", range(2))
+def test_oracle_lookup_matches_reference_fragment_code(oracle, reference, case):
+    """cfo_lookup_clusters' cluster, count, offset and LinearDepth ==
+    Scene.frag:54-78 compiled as C++ (a fragment past the grid reads a zero
+    cell there, and is flagged OUTSIDE_GRID with count 0 here)."""
+    from hellovulkan_gb300._lib import FRAGMENT_OUTSIDE_GRID
+    v = _fragment_views()[case]
+    a = oracle.generate_aabbs(v.ubo)
+    cells, idx, _ = oracle.cull(v.ubo, a, v.lights, 150)
+    w, h = int(v.ubo.screenSize[0]), int(v.ubo.screenSize[1])
+    depth = scenes.depth_log_uniform(np.random.default_rng(5 + case), w, h, float(v.ubo.cameraNear),
+                                     float(v.ubo.cameraFar), far_plane_fraction=0.02)
+    depth[0, :10] = 0.0
+    got = oracle.lookup_clusters(v.ubo, depth, cells, idx, v.lights, 150, a)
+    ref = reference.lookup_fragments(v.ubo, depth, cells, threads=4)
+    inside = ref["cluster"] < cells.shape[0]
+    assert np.array_equal((got["flags"] & FRAGMENT_OUTSIDE_GRID) == 0, inside)
+    assert np.array_equal(got["cluster"][inside], ref["cluster"][inside])
+    assert np.array_equal(got["count"], ref["count"]) and np.array_equal(got["offset"], ref["offset"])
+    assert np.array_equal(bits(got["linear_depth"]), bits(ref["linear_depth"]))
+    assert inside.mean() > 0.9 and (~inside).any()
+
+
+@pytest.mark.parametrize("case", range(2))
+def test_oracle_shading_matches_reference_fragment_code(oracle, reference, case):
+    """cfo_shade_clusters' Lo == Scene.frag's direct lighting (Radiance.glsl
+    and PBRHeader.glsl) compiled as C++, bit for bit; alpha is 1 exactly where
+    the lookup lands in the grid."""
+    from hellovulkan_gb300._lib import CfPBRPushConstant
+    v = _fragment_views()[case]
+    a = oracle.generate_aabbs(v.ubo)
+    cells, idx, _ = oracle.cull(v.ubo, a, v.lights, 150)
+    g = scenes.gbuffer(np.random.default_rng(9 + case), v.ubo, far_plane_fraction=0.02)
+    cam = scenes.camera_position(v.ubo)
+    pc = CfPBRPushConstant(*PC_DEFAULT)
+    got = oracle.shade_clusters(v.ubo, cam, pc, g, cells, idx, v.lights)
+    rgb, cl = reference.shade_fragments(v.ubo, cam, pc, g, cells, idx, v.lights, threads=4)
+    assert np.array_equal(bits(got[..., :3]), bits(rgb))
+    assert np.array_equal(got[..., 3] == 1.0, cl < cells.shape[0])
+
+
+def test_oracle_shading_signed_zero_matches_reference(oracle, reference):
+    """Radiance's own Lo starts at vec3(0.0) (Radiance.glsl:13,55), so a light
+    whose term is -0 (NoL = -0: N = -z, the light in the texel's plane) adds
+    +0: with albedoMultipler -0.0, Scene.frag's Lo ends +0, not -0."""
+    from hellovulkan_gb300._lib import CfPBRPushConstant
+    v = scenes.custom_view((1, 1, 1), 4, 4, 0.1, 100.0)
+    g = np.zeros((4, 4, 12), np.float32)
+    g[..., 0:3] = (0.0, 0.0, -5.0)
+    g[..., 3] = 0.5
+    g[..., 4:7] = (0.0, 0.0, -1.0)
+    g[..., 7] = 0.3
+    g[..., 8:11] = (-0.0, 0.25, 0.5)
+    g[..., 11] = 0.6
+    L = scenes.make_lights(np.float32([[-1.0, -1.0, -5.0]]), np.float32([10.0]))
+    cells, idx = np.array([[0, 1]], np.uint32), np.array([0], np.uint32)
+    for mult in (0.0, -0.0, 0.1):
+        pc = CfPBRPushConstant(1.75, 0.01, 0.0, 0.1, mult)
+        got = oracle.shade_clusters(v.ubo, np.zeros(3), pc, g, cells, idx, L)
+        rgb, _ = reference.shade_fragments(v.ubo, np.zeros(3), pc, g, cells, idx, L)
+        assert np.array_equal(bits(got[..., :3]), bits(rgb)), mult
+    assert not np.signbit(got[..., :3]).any()
+
+
+def test_oracle_consumers_match_golden(oracle, golden_consumers):
+    """The oracle's frustum culling, lookup and lighting against the outputs
+    the reference's own shader code produced (golden_consumers.npz)."""
+    from hellovulkan_gb300._lib import CfFrustum, CfPBRPushConstant, FRAGMENT_OUTSIDE_GRID
+    g = golden_consumers
+    boxes = g["frustum/boxes"]
+    for k in range(3):
+        f = CfFrustum.from_buffer_copy(g["frustum/f%d" % k].tobytes())
+        assert np.array_equal(oracle.frustum_cull(f, boxes), g["frustum/instance%d" % k].astype(np.uint32)), k
+    ubo = ubo_from_bytes(g["frag/ubo"])
+    cells, idx, lights = g["frag/cells"], g["frag/indices"], g["frag/lights"]
+    s = oracle.lookup_clusters(ubo, g["frag/depth"], cells, idx, lights, 150)
+    inside = g["frag/lookup_cluster"] < cells.shape[0]
+    assert np.array_equal((s["flags"] & FRAGMENT_OUTSIDE_GRID) == 0, inside)
+    assert np.array_equal(s["cluster"][inside], g["frag/lookup_cluster"][inside])
+    assert np.array_equal(s["count"], g["frag/lookup_count"]) and np.array_equal(s["offset"], g["frag/lookup_offset"])
+    assert np.array_equal(bits(s["linear_depth"]), g["frag/lookup_linear_depth"])
+    out = oracle.shade_clusters(ubo, g["frag/camera"], CfPBRPushConstant(*g["frag/pc"].tolist()), g["frag/gbuffer"],
+                                cells, idx, lights)
+    assert np.array_equal(bits(out[..., :3]), g["frag/shade_rgb"])
+    assert np.array_equal(out[..., 3] == 1.0, g["frag/shade_cluster"] < cells.shape[0])
+    out = oracle.shade_clusters(ubo_from_bytes(g["negzero/ubo"]), np.zeros(3), CfPBRPushConstant(
+        *g["negzero/pc"].tolist()), g["negzero/gbuffer"], g["negzero/cells"], g["negzero/indices"], g["negzero/lights"])
+    assert np.array_equal(bits(out[..., :3]), g["negzero/shade_rgb"])

@@ -47,8 +47,8 @@ METRIC = "light-cluster tests/s"
 UNIT = "tests/s"
 OPS_PER_TEST = 16
 L2_FLUSH_BYTES = 256 << 20
-SMS = 152
 FP32_LANES_PER_SM = 128
+REF_BUDGET_S = 150.0  # the reference arm's whole run stays within this
 PLAIN_SMALL = (1, 8, 512, 4, 0)  # brute-force culling configurations
 PLAIN_LARGE = (2, 8, 512, 4, 0)
 
@@ -82,12 +82,19 @@ def make_view(name: str, rank: int):
 
 
 def workload_config(view, name):
+    """The workload only (the same dict in both arms); how it is measured
+    goes under the line's "measurement" key."""
     x, y, z = view.grid
     w, h = view.ubo.screenSize
     return {"workload": "%s: %dx%d, grid %dx%dx%d = %d clusters, %d lights, cap %d" % (
         name, w, h, x, y, z, view.clusters, view.light_count, view.cap),
         "clusters": view.clusters, "lights": view.light_count, "cap": view.cap,
         "tests_per_view": view.clusters * view.light_count}
+
+
+def fp32_peak_tops(sm_count: int, sm_mhz: float) -> float:
+    """Nominal FP32 issue rate: SMs x 128 lanes x SM clock, in Tops/s."""
+    return sm_count * FP32_LANES_PER_SM * sm_mhz * 1e6 / 1e12
 
 
 def dist_env():
@@ -184,18 +191,18 @@ def cpu_threads() -> int:
 
 
 def time_cpu(view, aabbs, budget_s: float, steps: int | None = None, warmup: int = 1):
-    """Times the CPU implementation on slice samples; returns a dict."""
+    """Times the CPU implementation, each step the whole view when
+    (warmup + steps) whole views fit the budget, else a run of depth slices
+    sized to it; returns a dict."""
     kind, cull = cpu_impl()
     threads = cpu_threads()
     X, Y, Z = view.grid
-    # size the per-step sample: as many depth slices as fit the budget
-    u1, a1 = sub_view(view.ubo, aabbs, 0, 1)
     t0 = time.perf_counter()
-    cull(u1, a1, view.lights, view.cap, threads)
-    one = max(time.perf_counter() - t0, 1e-4)
+    cull(view.ubo, aabbs, view.lights, view.cap, threads)  # one whole view: sizes the sample, warms the caches
+    full = max(time.perf_counter() - t0, 1e-4)
     n_steps = steps if steps is not None else 5
-    per_step = budget_s / max(n_steps, 1)
-    nz = int(max(1, min(Z, per_step / one)))
+    per_step = budget_s / max(n_steps + warmup, 1)
+    nz = Z if full <= per_step else int(max(1, min(Z, per_step / (full / Z))))
     times, tests = [], 0
     for i in range(warmup + n_steps):
         k0 = (i * nz) % max(1, Z - nz + 1)
@@ -220,13 +227,13 @@ def run_reference_arm(args):
     from oracle import Oracle
     view = make_view(args.workload, 0)
     aabbs = Oracle().generate_aabbs(view.ubo)
-    budget = min(150.0, max(10.0, 0.05 * (args.steps + args.warmup)))
-    r = time_cpu(view, aabbs, budget, steps=args.steps, warmup=args.warmup)
+    r = time_cpu(view, aabbs, REF_BUDGET_S, steps=args.steps, warmup=args.warmup)
     cfg = workload_config(view, args.workload)
     line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "impl": "reference",
             "config": cfg,
+            "measurement": {"sample": r["sample"], "timing": "host clock per step, all host threads"},
             "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": r["kind"],
                              "sample": r["sample"]},
             "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -355,6 +362,95 @@ def measure_batch(ctx, stream, n_views=256, passes=20, seed=3, sample_views=6):
         "items": info["items"], "parity_sampled_views": parity, "sampled_views": sample,
         "l2": "inputs larger than L2 (%.0f MB of buffers), no flush" % (bufs.device_bytes / 1e6),
     }
+
+
+def event_floor_ms(stream, flush, reps):
+    """The same bracket as a timed step (L2 flush, start event, work, end
+    event) around one 1-element torch kernel: the part of an event-timed step
+    that is not the step's own kernels."""
+    import torch
+    tiny = torch.zeros(1, device="cuda")
+    out = []
+    for _ in range(reps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        with torch.cuda.stream(stream):
+            tiny.add_(1.0)
+        b.record(stream)
+        torch.cuda.synchronize()
+        out.append(a.elapsed_time(b))
+    return float(np.median(out))
+
+
+def measure_plain_small(ctx, stream, flush, steps, warmup, rank, sm_count, sm_mhz, traffic):
+    """The 1920x1080, 16x9x24-cluster view with 1024 lights through
+    PipelineLightCulling: one launch per view (the one-launch kernel).  Each
+    step is event-timed on the launching stream with L2 flushed before it;
+    event_floor_ms is the same bracket around a 1-element kernel.  The FP32
+    fraction counts the reference loop's executed tests x 16 ops against the
+    step, and against the step less that floor."""
+    import torch
+
+    from hellovulkan_gb300 import scenes
+    from hellovulkan_gb300.pipelines import (PipelineAABBGenerator, PipelineLightCulling, ResourcesClusterForward,
+                                             ResourcesLight)
+    from oracle import Oracle
+    v = scenes.plain_small(1 + 1000 * rank)
+    rl = ResourcesLight(ctx)
+    rl.add_lights(v.lights)
+    rc = ResourcesClusterForward(ctx)
+    rc.create_buffers(*v.grid, v.cap)
+    gen = PipelineAABBGenerator(ctx, rc)
+    gen.set_cluster_forward_ubo(v.ubo)
+    gen.fill_command_buffer(stream)
+    cu = PipelineLightCulling(ctx, rl, rc)
+    cu.set_cluster_forward_ubo(v.ubo)
+    tuning = cu.tuning()
+    for _ in range(max(3, warmup)):
+        cu.fill_command_buffer(stream)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for i in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        starts[i].record(stream)
+        cu.fill_command_buffer(stream)
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    step_ms = float(np.mean(ms))
+    floor_ms = event_floor_ms(stream, flush, max(10, min(steps, 100)))
+    cells, idx = rc.read_outputs(stream)
+    o = Oracle()
+    oa = o.generate_aabbs(v.ubo)
+    oc, oi, executed = o.cull(v.ubo, oa, v.lights, v.cap)
+    parity = bool(np.array_equal(cells, oc) and np.array_equal(idx, oi))
+    for obj in (cu, gen, rc, rl):
+        obj.close()
+    peak = fp32_peak_tops(sm_count, sm_mhz)
+    ops = executed * OPS_PER_TEST
+    ach = ops / (step_ms * 1e-3) / 1e12
+    kernel_ms = max(step_ms - floor_ms, 1e-6)
+    ach_k = ops / (kernel_ms * 1e-3) / 1e12
+    kname = ("one_launch_kernel (%d clusters per CTA, %d warps)" % (tuning[0], tuning[1]) if tuning[4] == 2 else
+             "cull_kernel<%d,%d,%d,%d> + transform + copy" % tuple(tuning[:4]))
+    return {"workload": workload_config(v, "plain_small")["workload"],
+            "tuning": list(tuning), "kernels_per_step": 1 if tuning[4] == 2 else 3,
+            "ms_per_step": step_ms, "ms_per_step_min": float(np.min(ms)), "steps": steps,
+            "value": v.clusters * v.light_count / (step_ms * 1e-3), "unit": UNIT,
+            "views_per_s": 1e3 / step_ms, "parity_with_oracle": parity,
+            "event_floor_ms": floor_ms,
+            "executed_tests_per_view_reference_loop": executed,
+            "roofline": {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "Tops/s", "frac": ach / peak,
+                         "kernel": kname, "ops_per_launch": ops, "traffic": traffic.get("one_launch_kernel"),
+                         "peak_source": "nominal FP32 issue rate, %d SMs (device attribute) x %d lanes x %.0f MHz" % (
+                             sm_count, FP32_LANES_PER_SM, sm_mhz),
+                         "note": "executed tests x 16 ops over the event-timed step (one launch)"},
+            "roofline_less_event_floor": {"achieved": ach_k, "frac": ach_k / peak, "kernel_ms": kernel_ms,
+                                          "note": "the same ops over the step less event_floor_ms"},
+            "l2": "flushed between timed steps (256 MiB write)"}
 
 
 HOST_STALL_MS = 10.0
@@ -631,6 +727,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
     from hellovulkan_gb300 import build as cuda_build
     cuda_build.build()
     from hellovulkan_gb300.pipelines import (Context, PipelineAABBGenerator, PipelineLightCulling,
@@ -771,6 +868,16 @@ def run_ours(args):
     _, plain_stage = timed_steps(max(3, min(plain_steps, 50)), stages=True)
     cull.set_tuning(0)
 
+    traffic_all = {}
+    try:
+        traffic_all = json.loads((REPO / "profiles" / "dram_bytes_per_launch.json").read_text())
+    except (OSError, ValueError):
+        traffic_all = {}
+    small = None
+    if args.workload == "plain_large" and rank == 0:  # the 1920x1080 view, one launch per view
+        small = measure_plain_small(ctx, stream, flush, max(3, args.steps), args.warmup, rank, sm_count,
+                                    clocks.get("sm_max_mhz") or 2070.0, traffic_all.get("plain_small", {}))
+
     batched = None
     if not args.no_batch and rank == 0:
         batched = measure_batch(ctx, stream)
@@ -806,14 +913,17 @@ def run_ours(args):
         np.array_equal(p[4], o_cells) and np.array_equal(p[5][: o_idx.size], o_idx) for p in pipes)
 
     value = ws * tests_per_view * args.steps / (total_ms * 1e-3)
-    gw = cull_cfg_used[0] * cull_cfg_used[1]
     X, Y, Z = view.grid
-    groups = Z * -(-(X * Y) // gw) if cull_cfg_used[4] else -(-view.clusters // gw)
-    kernels_per_step = (4 if cull_cfg_used[4] else 3) + (1 if groups > 8192 else 0)
+    if cull_cfg_used[4] == 2:  # the one-launch kernel
+        kernels_per_step = 1
+    else:
+        gw = cull_cfg_used[0] * cull_cfg_used[1]
+        groups = Z * -(-(X * Y) // gw) if cull_cfg_used[4] else -(-view.clusters // gw)
+        kernels_per_step = (4 if cull_cfg_used[4] else 3) + (1 if groups > 8192 else 0)
     sm_max = clocks.get("sm_max_mhz") or 2070.0
-    fp32_peak = SMS * FP32_LANES_PER_SM * sm_max * 1e6 / 1e12
-    peak_note = ("nominal FP32 issue rate, %d SMs x %d lanes x %.0f MHz (no measured FP32 peak exists in "
-                 "MEASURED_PEAKS.json)" % (SMS, FP32_LANES_PER_SM, sm_max))
+    fp32_peak = fp32_peak_tops(sm_count, sm_max)
+    peak_note = ("nominal FP32 issue rate, %d SMs (device attribute) x %d lanes x %.0f MHz (no measured FP32 peak "
+                 "exists in MEASURED_PEAKS.json)" % (sm_count, FP32_LANES_PER_SM, sm_max))
     peaks = {}
     try:
         peaks = json.loads((REPO / "MEASURED_PEAKS.json").read_text())
@@ -832,8 +942,11 @@ def run_ours(args):
     cull_ops = (work_filter + work_cluster) * OPS_PER_TEST
     fin_bytes = 12 * view.clusters + 8 * H
     auto_cfg = cull_cfg_used
-    cull_kernel_name = ("bin_slices_kernel + cull_pipe_kernel<%d,%d,%d,%d> (binned)" if auto_cfg[4] else
-                        "cull_kernel<%d,%d,%d,%d> (brute force)") % tuple(auto_cfg[:4])
+    if auto_cfg[4] == 2:
+        cull_kernel_name = "one_launch_kernel (%d clusters per CTA, %d warps)" % tuple(auto_cfg[:2])
+    else:
+        cull_kernel_name = ("bin_slices_kernel + cull_pipe_kernel<%d,%d,%d,%d> (binned)" if auto_cfg[4] else
+                            "cull_kernel<%d,%d,%d,%d> (brute force)") % tuple(auto_cfg[:4])
     if st_c >= st_f:
         ach = cull_ops / (st_c * 1e-3) / 1e12
         roof = {"bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "Tops/s", "frac": ach / fp32_peak,
@@ -864,14 +977,16 @@ def run_ours(args):
         cpu = {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": r["kind"], "sample": r["sample"],
                "cpu": r["cpu"]}
     cfg = workload_config(view, args.workload)
-    cfg.update({"parallelism": "replicas x%d" % ws if ws > 1 else "single GPU",
-                "l2": "flushed between timed steps (256 MiB write)",
-                "aabbs": "generated once per projection (%.4f ms, not in the step)" % aabb_ms,
-                "step": "light transform + slice binning + culling + offset scan"})
+    measurement = {"parallelism": "replicas x%d" % ws if ws > 1 else "single GPU",
+                   "l2": "flushed between timed steps (256 MiB write)",
+                   "aabbs": "generated once per projection (%.4f ms, not in the step)" % aabb_ms,
+                   "step": ("light transform + culling + offset scan in one launch" if auto_cfg[4] == 2 else
+                            "light transform + slice binning + culling + offset scan"),
+                   "sm_count": sm_count}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded)", "config": cfg,
+        "dtype": "f32", "data": "synthetic (seeded)", "config": cfg, "measurement": measurement,
         "views_per_s": ws * args.steps / (total_ms * 1e-3),
         "parity_with_oracle": parity,
         "stage_ms": {"light_transform": st_x, "bin_and_cull": st_c, "offset_scan": st_f},
@@ -895,7 +1010,9 @@ def run_ours(args):
                               in_flight, in_flight - 1)},
         # our kernels per step: light transform, [slice binning,] culling, [offset scan, for views of more
         # than 8192 cluster groups,] copy; each e2e step adds the read-back kernel (both e2e runs are timed)
-        "gpu_launches": kernels_per_step * args.steps + (kernels_per_step + 1) * 2 * e2e_steps,
+        "gpu_launches": kernels_per_step * args.steps + (kernels_per_step + 1) * 2 * e2e_steps + (
+            small["kernels_per_step"] * small["steps"] if small else 0),
+        "plain_small": small,
         "clocks": clocks,
         "batched": batched,
         "served": served,

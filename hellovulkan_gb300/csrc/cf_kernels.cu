@@ -29,6 +29,7 @@
 // Floating point follows include/cf_pinned_math.h: every product and sum is an
 // explicit round-to-nearest intrinsic, so nothing is contracted into an FMA.
 #include "cf_kernels.cuh"
+#include "cf_device.cuh"
 
 #include <algorithm>
 #include <utility>
@@ -38,10 +39,6 @@
 namespace cfk {
 namespace {
 
-constexpr unsigned kFull = 0xffffffffu;
-constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per bounded wait
-constexpr uint32_t kWaitLimitIters = 1u << 26;
-
 // ---------------------------------------------------------------------------
 // PTX helpers: mbarrier and bulk async copy.
 // ---------------------------------------------------------------------------
@@ -50,12 +47,6 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p)
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-__device__ __forceinline__ uint64_t global_timer_ns()
-{
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
 
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
 {
@@ -133,15 +124,6 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-// Programmatic dependent launch.  The kernels of one view's step are launched
-// with programmatic stream serialisation, so each may be scheduled while the
-// previous kernel of the stream is still running: it runs only its prologue
-// (barrier init, parameters) before grid_dependency_wait(), which returns
-// once every earlier kernel of the stream has completed and its writes are
-// visible.  launch_dependents() lets the next kernel be scheduled early.
-// Both are no-ops in a launch without a programmatic dependency.
-__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 // Named barrier 1 over the first N threads of the CTA (the consumer warps;
 // the producer warp never takes part).
@@ -151,34 +133,6 @@ __device__ __forceinline__ void consumer_sync()
     asm volatile("bar.sync 1, %0;" ::"n"(N) : "memory");
 }
 
-__device__ __forceinline__ float max3f(float a, float b, float c)
-{
-    float r;
-    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
-}
-
-__device__ __forceinline__ bool finite_bits(float x)
-{
-    return (__float_as_uint(x) & 0x7f800000u) != 0x7f800000u;
-}
-
-__device__ __forceinline__ uint32_t warp_sum(uint32_t x)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
-    return x;
-}
-
-__device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t x, uint32_t lane)
-{
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(kFull, x, o);
-        if (lane >= (uint32_t)o) x += y;
-    }
-    return x;
-}
 
 // ---------------------------------------------------------------------------
 // AABB generator: AABBGenerator.comp:39-89, one thread per cluster.
@@ -320,45 +274,8 @@ __global__ void __launch_bounds__(256) batch_aabb_kernel(const AabbJob* __restri
 }
 
 // ---------------------------------------------------------------------------
-// Culling.
+// Culling (the sphere-box tests hit_fast / hit_exact are in cf_device.cuh).
 // ---------------------------------------------------------------------------
-
-// Exact for every finite light coordinate against boxes with min <= max on
-// each axis (or NaN bounds), which every generated AABB satisfies:
-//   v < min:  max3(min - v, v - max, 0) = min - v
-//   v > max:  = v - max, and (v - max)^2 == (max - v)^2 bit for bit
-//   inside:   both differences are <= 0, so d = 0 and the axis adds +0,
-//             which leaves the reference's partial sum unchanged
-// NaN bounds are ignored by max.f32 exactly like the reference's false
-// comparisons.  Boxes set to +inf on every bound never hit (the capped and
-// out-of-range clusters).
-__device__ __forceinline__ bool hit_fast(const float4& L, const float* mn, const float* mx)
-{
-    const float dx = max3f(__fsub_rn(mn[0], L.x), __fsub_rn(L.x, mx[0]), 0.0f);
-    const float dy = max3f(__fsub_rn(mn[1], L.y), __fsub_rn(L.y, mx[1]), 0.0f);
-    const float dz = max3f(__fsub_rn(mn[2], L.z), __fsub_rn(L.z, mx[2]), 0.0f);
-    const float sq = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-    return sq < L.w;
-}
-
-// SquaredDistancePointAABB + TestSphereAABB (LightCulling.comp:26-57) as
-// written, for granules holding a non-finite light coordinate.
-__device__ __forceinline__ bool hit_exact(const float4& L, const float* mn, const float* mx)
-{
-    const float v[3] = {L.x, L.y, L.z};
-    float sq = 0.0f;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        if (v[a] < mn[a]) {
-            const float d = __fsub_rn(mn[a], v[a]);
-            sq = __fadd_rn(sq, __fmul_rn(d, d));
-        } else if (v[a] > mx[a]) {
-            const float d = __fsub_rn(mx[a], v[a]);
-            sq = __fadd_rn(sq, __fmul_rn(d, d));
-        }
-    }
-    return sq < L.w;
-}
 
 template <int K>
 struct WarpClusters {
@@ -1531,6 +1448,9 @@ cudaError_t launch_cull_t(const ViewCull& v, uint32_t* dev_error, cudaStream_t s
 
 bool cull_config_supported(const CullConfig& c)
 {
+    if (c.binned == kModeOneLaunch)
+        return c.clusters_per_warp >= 1 && (uint32_t)c.clusters_per_warp <= kOneLaunchMaxClustersPerCta &&
+               c.stages == 1 && one_launch_shape_supported(c.warps, c.tile);
 #define CF_MATCH(K, W, T, S, B) \
     if (c.clusters_per_warp == K && c.warps == W && c.tile == T && c.stages == S && (c.binned != 0) == B) return true;
     CF_CULL_CONFIGS(CF_MATCH)
@@ -1539,25 +1459,37 @@ bool cull_config_supported(const CullConfig& c)
 }
 
 // Slice binning pays off once a view has enough tests to amortise its extra
-// launch and passes: on a GB300 the 1920x1080 16x9x24 view with 1024 lights
-// (3.5 M tests) culls faster brute force, the 2560x1600 32x18x48 view with
-// 16384 lights (453 M tests) five times faster binned.
+// launch and passes: on a GB300 the 2560x1600 32x18x48 view with 16384
+// lights (453 M tests) culls five times faster binned than brute force.
+// Below that, a view whose lights fit one launch's registers (at most
+// kOneLaunchMaxLights) and whose clusters spread over the resident CTAs at
+// most kOneLaunchMaxClustersPerCta each is culled in one launch; the rest
+// brute force.
 constexpr uint64_t kBinnedMinTests = 16ull << 20;
 
 CullConfig default_cull_config(uint32_t clusters, uint32_t lights, uint32_t slices)
 {
     if (slices >= 2 && (uint64_t)clusters * lights >= kBinnedMinTests) return CullConfig{2, 8, 1024, 2, 1};
+    CullConfig one{};
+    if (one_launch_config(clusters, lights, &one)) return one;
     if (clusters <= 8192) return CullConfig{1, 8, 512, 4, 0};
     return CullConfig{2, 8, 512, 4, 0};
 }
 
-WorkspaceLayout workspace_layout(uint32_t clusters, uint32_t lights, uint32_t cap, uint32_t slices, bool binned,
+WorkspaceLayout workspace_layout(uint32_t clusters, uint32_t lights, uint32_t cap, uint32_t slices, int mode,
                                  uint32_t groups)
 {
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     WorkspaceLayout w{};
-    const uint32_t lpad = pad_lights(lights);
     size_t off = 256;  // status words
+    if (mode == kModeOneLaunch) {
+        w.partials = off;
+        off += al((size_t)groups * sizeof(unsigned long long));
+        w.bytes = off;
+        return w;
+    }
+    const bool binned = mode == kModeBinned;
+    const uint32_t lpad = pad_lights(lights);
     w.vlights = off;
     off += al((size_t)lpad * sizeof(float4));
     w.nonfinite = off;

@@ -32,6 +32,12 @@ constexpr uint32_t kFlagGranule = 256;   // lights per non-finite flag word
 // Device error codes (OR-ed into the context's error word).
 constexpr uint32_t kErrFullWaitTimeout = 1u << 0;   // a consumer waited too long for a light tile
 constexpr uint32_t kErrEmptyWaitTimeout = 1u << 1;  // the producer waited too long for a free stage
+constexpr uint32_t kErrLookbackTimeout = 1u << 2;   // a one-launch CTA waited too long for an earlier CTA's total
+
+// Culling modes (CullConfig::binned).
+constexpr int kModeBruteForce = 0;  // transform, every light against every cluster, copy
+constexpr int kModeBinned = 1;      // transform, slice binning, persistent culling of the candidates, copy
+constexpr int kModeOneLaunch = 2;   // everything in one launch (cf_fused.cu), views of up to kOneLaunchMaxLights
 
 inline uint32_t pad_lights(uint32_t n) { return (n + kLightPad - 1) / kLightPad * kLightPad; }
 inline uint32_t granules(uint32_t lpad) { return (lpad + kFlagGranule - 1) / kFlagGranule; }
@@ -105,30 +111,79 @@ __host__ __device__ inline void group_range(const ViewCull& v, uint32_t b, uint3
     }
 }
 
-inline uint32_t group_count(uint32_t clusters, uint32_t slice_clusters, uint32_t slices, uint32_t gw, bool binned)
+inline uint32_t group_count(uint32_t clusters, uint32_t slice_clusters, uint32_t slices, uint32_t gw, int mode)
 {
-    return binned ? slices * ((slice_clusters + gw - 1) / gw) : (clusters + gw - 1) / gw;
+    return mode == kModeBinned ? slices * ((slice_clusters + gw - 1) / gw) : (clusters + gw - 1) / gw;
 }
 
 // One culling configuration: clusters per warp, consumer warps per CTA,
-// lights per shared-memory stage, number of stages.
+// lights per shared-memory stage, number of stages, mode.  A one-launch
+// configuration reads them as clusters per CTA, warps per CTA, the most
+// lights it takes (32 per warp and chunk), and 1.
 struct CullConfig {
     int clusters_per_warp;
     int warps;
     int tile;
     int stages;
-    int binned;  // 0: every light against every cluster; 1: slice candidate lists first
+    int binned;  // kModeBruteForce, kModeBinned or kModeOneLaunch
 };
 
-// Workspace carve-up for one view (cf_cull_lights).
+// Clusters one culling CTA owns (a cluster group).
+inline uint32_t group_width(const CullConfig& c)
+{
+    return c.binned == kModeOneLaunch ? (uint32_t)c.clusters_per_warp : (uint32_t)(c.warps * c.clusters_per_warp);
+}
+
+// Workspace carve-up for one view (cf_cull_lights).  A one-launch view needs
+// only the status block and one 8-byte word per CTA (`partials`).
 struct WorkspaceLayout {
     size_t vlights, nonfinite, counts, staging, group_sums, group_offsets, slice_lights, slice_idx, slice_count,
-        slice_nonfinite, group_boxes, bytes;
+        slice_nonfinite, group_boxes, partials, bytes;
 };
-constexpr size_t kQueueWord = 64;  // byte offset, in a workspace's status block, of the single-view item counter
+constexpr size_t kQueueWord = 64;   // byte offset, in a workspace's status block, of the single-view item counter
+constexpr size_t kEpochWord = 128;  // byte offset of the one-launch kernel's epoch (see FusedCull)
 // Scratch of one view; `groups` = group_count(...) of the configuration used.
-WorkspaceLayout workspace_layout(uint32_t clusters, uint32_t lights, uint32_t cap, uint32_t slices, bool binned,
+WorkspaceLayout workspace_layout(uint32_t clusters, uint32_t lights, uint32_t cap, uint32_t slices, int mode,
                                  uint32_t groups);
+
+// One-launch culling of a small view (cf_fused.cu): light transform,
+// LightCulling.comp's test for every (cluster, light) pair, the capped
+// ordered lists, the cluster-order offsets and the packed output, all in one
+// cooperative launch.  CTA b owns clusters [b*per_cta, (b+1)*per_cta); its
+// warps transform their share of the lights into registers and test them
+// against the CTA's clusters; each test's 32 results are one ballot mask.
+// The CTA's capped hit total goes to partials[b] as (tag << 32) | total, and
+// each CTA sums the totals of the CTAs before it: that is its output offset.
+// The tag is *epoch + 1, read at kernel start; the last CTA stores it back
+// into *epoch once every CTA has published (so each CTA has read the old
+// value), and words from earlier launches never carry the current tag.  The
+// workspace must be zero-filled once after allocation.
+struct FusedCull {
+    const CfLightData* lights;
+    const float4* aabbs;
+    CfLightCell* cells;
+    uint32_t* indices;
+    uint32_t* total;                // may be null
+    unsigned long long* partials;   // ctas words
+    uint32_t* epoch;
+    unsigned long long* work;       // optional work counters (see ViewCull)
+    float view[16];                 // cameraView, column-major
+    uint32_t light_count;
+    uint32_t clusters;
+    uint32_t cap;
+    uint32_t per_cta;               // clusters per CTA, <= kOneLaunchMaxClustersPerCta
+    uint32_t ctas;
+};
+constexpr uint32_t kOneLaunchMaxLights = 2048;
+constexpr uint32_t kOneLaunchMaxClustersPerCta = 32;
+constexpr uint32_t kOneLaunchMaxCtas = 256;
+// The compiled one-launch shapes: (warps per CTA, most lights) = (32, 1024), (16, 2048), (16, 1024).
+bool one_launch_shape_supported(int warps, int max_lights);
+// CTAs of that shape that can be resident at once on the current device.
+cudaError_t one_launch_resident_ctas(int warps, int max_lights, int* ctas);
+// The one-launch configuration for a view, if one fits (false otherwise).
+bool one_launch_config(uint32_t clusters, uint32_t lights, CullConfig* cfg);
+cudaError_t launch_one_launch(const FusedCull& f, int warps, int max_lights, uint32_t* dev_error, cudaStream_t stream);
 
 bool cull_config_supported(const CullConfig& c);
 CullConfig default_cull_config(uint32_t clusters, uint32_t lights, uint32_t slices);

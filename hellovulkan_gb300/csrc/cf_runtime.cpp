@@ -131,8 +131,8 @@ cfk::WorkspaceLayout layout_for(const CfClusterForwardUBO& ubo, uint32_t light_c
 {
     const uint32_t C = ubo.sliceCountX * ubo.sliceCountY * ubo.sliceCountZ;
     const uint32_t groups = cfk::group_count(C, ubo.sliceCountX * ubo.sliceCountY, ubo.sliceCountZ,
-                                             (uint32_t)(cfg.warps * cfg.clusters_per_warp), cfg.binned != 0);
-    return cfk::workspace_layout(C, light_count, cap, ubo.sliceCountZ, cfg.binned != 0, groups);
+                                             cfk::group_width(cfg), cfg.binned);
+    return cfk::workspace_layout(C, light_count, cap, ubo.sliceCountZ, cfg.binned, groups);
 }
 
 int enqueue_cull(const CfClusterForwardUBO& ubo, const CfAABB* d_aabbs, const CfLightData* d_lights,
@@ -142,6 +142,33 @@ int enqueue_cull(const CfClusterForwardUBO& ubo, const CfAABB* d_aabbs, const Cf
 {
     const uint32_t C = ubo.sliceCountX * ubo.sliceCountY * ubo.sliceCountZ;
     const cfk::WorkspaceLayout L = layout_for(ubo, light_count, cap, cfg);
+    if (cfg.binned == cfk::kModeOneLaunch) {
+        if (light_count > (uint32_t)cfg.tile)
+            return fail(CF_ERROR_INVALID_ARGUMENT, "%u lights exceed the %d of this one-launch configuration",
+                        light_count, cfg.tile);
+        cfk::FusedCull f{};
+        f.lights = d_lights;
+        f.aabbs = reinterpret_cast<const float4*>(d_aabbs);
+        f.cells = d_cells;
+        f.indices = d_indices;
+        f.total = d_total;
+        f.partials = reinterpret_cast<unsigned long long*>(ws + L.partials);
+        f.epoch = reinterpret_cast<uint32_t*>(ws + cfk::kEpochWord);
+        f.work = work;
+        for (int i = 0; i < 16; ++i) f.view[i] = ubo.cameraView[i];
+        f.light_count = light_count;
+        f.clusters = C;
+        f.cap = cap;
+        f.per_cta = cfk::group_width(cfg);
+        f.ctas = cfk::group_count(C, 0, 0, f.per_cta, cfg.binned);
+        cudaError_t e = stage_events ? cudaEventRecord(stage_events[0], stream) : cudaSuccess;
+        if (e == cudaSuccess && stage_events) e = cudaEventRecord(stage_events[1], stream);
+        if (e == cudaSuccess) e = cfk::launch_one_launch(f, cfg.warps, cfg.tile, dev_error, stream);
+        if (e != cudaSuccess) return cuda_fail(e, "one-launch culling");
+        if (stage_events) e = cudaEventRecord(stage_events[2], stream);
+        if (e == cudaSuccess && stage_events) e = cudaEventRecord(stage_events[3], stream);
+        return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "stage event");
+    }
     cfk::ViewCull v{};
     v.work = work;
     v.vlights = reinterpret_cast<const float4*>(ws + L.vlights);
@@ -158,8 +185,8 @@ int enqueue_cull(const CfClusterForwardUBO& ubo, const CfAABB* d_aabbs, const Cf
     v.slice_clusters = ubo.sliceCountX * ubo.sliceCountY;
     v.slices = ubo.sliceCountZ;
     v.binned = cfg.binned ? 1u : 0u;
-    v.group_width = (uint32_t)(cfg.warps * cfg.clusters_per_warp);
-    v.groups = cfk::group_count(C, v.slice_clusters, v.slices, v.group_width, cfg.binned != 0);
+    v.group_width = cfk::group_width(cfg);
+    v.groups = cfk::group_count(C, v.slice_clusters, v.slices, v.group_width, cfg.binned);
     v.group_sums = reinterpret_cast<uint32_t*>(ws + L.group_sums);
     v.group_offsets = reinterpret_cast<uint32_t*>(ws + L.group_offsets);
     if (cfg.binned) {
@@ -709,7 +736,9 @@ int cf_pipeline_light_culling_set_tuning(CfPipelineLightCulling* p, int clusters
         p->has_cfg = false;
         return CF_SUCCESS;
     }
-    const cfk::CullConfig c{clusters_per_warp, warps, tile, stages, binned ? 1 : 0};
+    if (binned < cfk::kModeBruteForce || binned > cfk::kModeOneLaunch)
+        return fail(CF_ERROR_INVALID_ARGUMENT, "culling mode %d (0 brute force, 1 binned, 2 one launch)", binned);
+    const cfk::CullConfig c{clusters_per_warp, warps, tile, stages, binned};
     if (!cfk::cull_config_supported(c))
         return fail(CF_ERROR_INVALID_ARGUMENT, "no culling kernel for K=%d warps=%d tile=%d stages=%d binned=%d",
                     clusters_per_warp, warps, tile, stages, binned);

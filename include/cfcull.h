@@ -174,15 +174,20 @@ CFCULL_API int cf_pipeline_light_culling_reset_global_index(CfPipelineLightCulli
 CFCULL_API int cf_pipeline_light_culling_set_cluster_forward_ubo(CfPipelineLightCulling* pipe,
                                                                  const CfClusterForwardUBO* ubo);
 /* PipelineLightCulling::FillCommandBuffer (PipelineLightCulling.cpp:51-119):
- * enqueues light transform, culling and the offset scan on `stream`. */
+ * enqueues light transform, culling and the offset scan on `stream` — for a
+ * small view (at most 2048 lights, clusters spread at most 32 per SM) all
+ * three in one kernel launch. */
 CFCULL_API int cf_pipeline_light_culling_fill_command_buffer(CfPipelineLightCulling* pipe, void* stream);
 
 /* Tuning: selects the culling kernel configuration (clusters per warp,
- * consumer warps per CTA, lights per shared-memory stage, stages, and
- * binned = 1 for the depth-slice candidate lists or 0 for every light against
- * every cluster); clusters_per_warp = 0 restores the automatic choice.
- * Unsupported combinations are rejected.  Every configuration gives the same
- * output. */
+ * consumer warps per CTA, lights per shared-memory stage, stages, and the
+ * mode: binned = 0 every light against every cluster, 1 the depth-slice
+ * candidate lists first, 2 the whole step in one launch, for which the
+ * arguments are clusters per CTA (1..32), warps per CTA, the most lights the
+ * launch takes and 1 — (M, 32, 1024, 1, 2), (M, 16, 2048, 1, 2) or
+ * (M, 16, 1024, 1, 2); a view with more lights than that is rejected when
+ * culled); clusters_per_warp = 0 restores the automatic choice.  Unsupported
+ * combinations are rejected.  Every configuration gives the same output. */
 CFCULL_API int cf_pipeline_light_culling_set_tuning(CfPipelineLightCulling* pipe, int clusters_per_warp, int warps,
                                                     int tile, int stages, int binned);
 /* The configuration the next fill_command_buffer uses (the override, or the

@@ -107,6 +107,12 @@ __device__ __forceinline__ unsigned long long ld_relaxed_gpu(const unsigned long
 
 // Predecessor totals a lane reads at most: kOneLaunchMaxCtas / 32.
 constexpr int kLookSlots = (int)(kOneLaunchMaxCtas / 32);
+// The CTAs publish within a fraction of a microsecond of each other, so a
+// poll right after a CTA's own publish mostly finds the earlier CTAs' old
+// words, and the polling traffic slows their stores: the first poll waits
+// about one L2 round trip, later ones a little less.  (On a GB300 this took
+// the wait from about 2.6 to 0.9 us on the 1920x1080 view.)
+constexpr unsigned kFirstPollDelayNs = 300, kRepollDelayNs = 100;
 
 // W warps per set, J chunks of 32 lights per warp, S sets splitting the boxes.
 template <int W, int J, int S>
@@ -275,13 +281,16 @@ __global__ void __launch_bounds__(W * S * 32) one_launch_kernel(const FusedCull 
         s_excl[lane] = incl - c;
         const uint32_t total = __shfl_sync(kFull, incl, 31);
         const uint32_t tag = s_tag;
-        if (lane == 0) st_relaxed_gpu(&f.partials[b], ((unsigned long long)tag << 32) | total);
+        // (a test may make CTA 0 withhold its total: the other CTAs' waits run out)
+        const bool withhold = b == 0 && (g_inject_stall & kInjectOneLaunchSkipPublish);
+        if (lane == 0 && !withhold) st_relaxed_gpu(&f.partials[b], ((unsigned long long)tag << 32) | total);
         uint32_t pending = 0, acc = 0;
 #pragma unroll
         for (int k = 0; k < kLookSlots; ++k)
             if (lane + 32u * k < b) pending |= 1u << k;
         bool ok = true;
         if (__any_sync(kFull, pending != 0)) {
+            __nanosleep(kFirstPollDelayNs);
             const uint64_t t0 = global_timer_ns();
             for (uint32_t it = 0; it < kWaitLimitIters; ++it) {
                 unsigned long long w[kLookSlots];
@@ -295,10 +304,11 @@ __global__ void __launch_bounds__(W * S * 32) one_launch_kernel(const FusedCull 
                         pending &= ~(1u << k);
                     }
                 if (!__any_sync(kFull, pending != 0)) break;
-                if (global_timer_ns() - t0 > kWaitLimitNs) {
+                if (global_timer_ns() - t0 > g_wait_limit_ns) {
                     ok = false;
                     break;
                 }
+                __nanosleep(kRepollDelayNs);
             }
             ok = __all_sync(kFull, ok && pending == 0);
         }
@@ -429,6 +439,15 @@ bool one_launch_config(uint32_t clusters, uint32_t lights, CullConfig* cfg)
         return false;
     *cfg = CullConfig{(int)per_cta, warps, max_lights, 1, kModeOneLaunch};
     return true;
+}
+
+cudaError_t set_test_knobs_one_launch(uint64_t wait_limit_ns, uint32_t inject)
+{
+    const unsigned long long w = wait_limit_ns;
+    const unsigned int i = inject;
+    cudaError_t e = cudaMemcpyToSymbol(g_wait_limit_ns, &w, sizeof(w));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_inject_stall, &i, sizeof(i));
+    return e;
 }
 
 cudaError_t launch_one_launch(const FusedCull& f, int warps, int max_lights, uint32_t* dev_error, cudaStream_t stream)

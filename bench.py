@@ -686,6 +686,20 @@ def measure_frustum(stream, reps=50):
     return out
 
 
+def check_stress_view(state, oracle):
+    """One animated view (StressAnimation.view_state) against the host
+    restatement of the orbit animation and the oracle's AABBs and culling."""
+    from oracle import animate_orbits
+    _, pos = animate_orbits(state["orbits0"], state["frame"])
+    lights = state["lights"]
+    oa = oracle.generate_aabbs(state["ubo"])
+    oc, oi, _ = oracle.cull(state["ubo"], oa, lights, state["cap"])
+    return {"frame": state["frame"], "view": state["view"],
+            "lights": bool(np.array_equal(lights[:, :4].view(np.uint32), pos.view(np.uint32))),
+            "aabbs": bool(np.array_equal(state["aabbs"].view(np.uint32), oa.view(np.uint32))),
+            "cells": bool(np.array_equal(state["cells"], oc)), "indices": bool(np.array_equal(state["indices"], oi))}
+
+
 def measure_stress(ctx, stream, n_views, n_lights, frames, seed=5):
     """The animated workload: n_views views x n_lights lights, every light moved
     one step along its orbit in place on the device each frame, every view
@@ -706,7 +720,9 @@ def measure_stress(ctx, stream, n_views, n_lights, frames, seed=5):
     setup_s = time.perf_counter() - t0
     check_frames = {f for f in (0, 59, 60, 61, 299, frames - 1) if 0 <= f < frames}
     check_views = sorted({0, 1, n_views // 2 + 1, n_views - 1})
-    rep = st.run(frames, stream, check_frames=check_frames, check_views=check_views, oracle=Oracle())
+    o = Oracle()
+    rep = st.run(frames, stream, check_frames=check_frames, check_views=check_views,
+                 check=lambda state: check_stress_view(state, o))
     st.close()
     del st
     torch.cuda.empty_cache()

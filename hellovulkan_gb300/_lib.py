@@ -229,6 +229,9 @@ _SIGS = {
     "cf_cull_lights": [C.POINTER(CfClusterForwardUBO), _P, _P, _U32, _U32, _P, _P, _U64, _P, _P, _U64, _P],
     "cf_cull_workspace_device_error": [_P, _PU32],
     "cf_cull_lights_static_scratch": [C.POINTER(CfClusterForwardUBO), _P, _P, _U32, _U32, _P, _P, _U64, _P, _P, _P],
+    "cf_testing_set_wait_limit_ns": [_U64],
+    "cf_testing_inject_stall": [_U32],
+    "cf_testing_fail_allocation_after": [C.c_int32],
     "cf_batch_create": [_P, C.POINTER(_P)],
     "cf_batch_destroy": [_P],
     "cf_batch_set_views": [_P, C.POINTER(CfBatchView), _U32],

@@ -332,7 +332,7 @@ int cf_batch_create(CfContext* ctx, CfBatch** out)
     b->device = context_device(ctx);
     b->dev_error = context_error_word(ctx);
     DeviceGuard g(b->device);
-    cudaError_t e = cudaMalloc(&b->d_queues, cfk::kMaxBatchQueues * sizeof(uint32_t));
+    cudaError_t e = device_malloc(reinterpret_cast<void**>(&b->d_queues), cfk::kMaxBatchQueues * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(b->d_queues, 0, cfk::kMaxBatchQueues * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->last_use, cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -398,6 +398,7 @@ int cf_batch_generate_aabbs(CfBatch* b, void* stream)
 
 int cf_batch_cull(CfBatch* b, void* stream)
 {
+    TraceRange trace("Batch_Light_Culling");
     if (!b) return fail(CF_ERROR_INVALID_ARGUMENT, "null batch");
     return batch_cull(b, (cudaStream_t)stream);
 }

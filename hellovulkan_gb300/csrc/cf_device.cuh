@@ -12,6 +12,18 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per bounded wait
 constexpr uint32_t kWaitLimitIters = 1u << 26;
 
+// Test knobs (include/cfcull_testing.h), one copy per translation unit that
+// includes this header: the library is built without relocatable device
+// code, so each file sets its own with set_test_knobs_*.
+//   g_wait_limit_ns  the time limit of every bounded wait (kWaitLimitNs
+//                    unless a test shortens it)
+//   g_inject_stall   0, or kInject* bits that make one CTA withhold a part
+//                    so that the others' bounded waits run out
+static __device__ unsigned long long g_wait_limit_ns = kWaitLimitNs;
+static __device__ unsigned int g_inject_stall = 0;
+constexpr unsigned kInjectOneLaunchSkipPublish = 1u;  // the one-launch kernel's CTA 0 does not publish its total
+constexpr unsigned kInjectBruteForceSkipTile = 2u;    // the brute-force kernel's CTA 0 producer never sends tile 0
+
 __device__ __forceinline__ uint64_t global_timer_ns()
 {
     uint64_t t;

@@ -81,15 +81,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
     return ok != 0;
 }
 
-// Waits for the phase of `parity` to complete; gives up after kWaitLimitNs
-// (or kWaitLimitIters polls) and returns false.
+// Waits for the phase of `parity` to complete; gives up after g_wait_limit_ns
+// (kWaitLimitNs unless a test shortens it) or kWaitLimitIters polls and
+// returns false.
 __device__ __noinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
 {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = global_timer_ns();
     for (uint32_t it = 0; it < kWaitLimitIters; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if (global_timer_ns() - t0 > kWaitLimitNs) break;
+        if (global_timer_ns() - t0 > g_wait_limit_ns) break;
     }
     return false;
 }
@@ -101,7 +102,7 @@ __device__ __noinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity, c
     const uint64_t t0 = global_timer_ns();
     for (uint32_t it = 0; it < kWaitLimitIters; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if (*abort || global_timer_ns() - t0 > kWaitLimitNs) break;
+        if (*abort || global_timer_ns() - t0 > g_wait_limit_ns) break;
     }
     return false;
 }
@@ -478,6 +479,8 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
         if (lane != 0) return;
         uint32_t t = 0;
         bool stalled = false;
+        // a test may make CTA 0 never send tile 0 (its consumers' waits run out)
+        const bool skip_first = group == 0 && (g_inject_stall & kInjectBruteForceSkipTile);
         for (; t < ntiles; ++t) {
             const uint32_t s = t % STAGES;
             if (t >= STAGES && !mbar_wait_bounded(smem_u32(&empty[s]), ((t / STAGES) & 1u) ^ 1u)) {
@@ -492,12 +495,17 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
                 break;
             }
             stop[s] = 0;
+            if (skip_first && t == 0) continue;  // no arrival and no copy for this tile
             const uint32_t n = min((uint32_t)TILE, nsrc - t * TILE);
             mbar_arrive_expect_tx(smem_u32(&full[s]), n * (uint32_t)sizeof(float4));
             bulk_copy_g2s(smem_u32(tiles + (size_t)s * TILE), v.vlights + (size_t)t * TILE,
                           n * (uint32_t)sizeof(float4), smem_u32(&full[s]));
         }
-        if (stalled)  // the last tile of each stage completes last
+        // After a stall, or with a tile withheld (the consumers may then leave
+        // before the copies land), wait for the copies in flight before the
+        // CTA can exit: the last tile of each stage completes last.  The
+        // withheld tile's wait runs out after the bounded time.
+        if (stalled || skip_first)
             for (uint32_t q = 0; q < STAGES && q < t; ++q) {
                 const uint32_t g = t - 1 - q;
                 mbar_wait_bounded(smem_u32(&full[g % STAGES]), (g / STAGES) & 1u);
@@ -1516,6 +1524,15 @@ WorkspaceLayout workspace_layout(uint32_t clusters, uint32_t lights, uint32_t ca
     }
     w.bytes = off;
     return w;
+}
+
+cudaError_t set_test_knobs_kernels(uint64_t wait_limit_ns, uint32_t inject)
+{
+    const unsigned long long w = wait_limit_ns;
+    const unsigned int i = inject;
+    cudaError_t e = cudaMemcpyToSymbol(g_wait_limit_ns, &w, sizeof(w));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_inject_stall, &i, sizeof(i));
+    return e;
 }
 
 cudaError_t launch_aabb(const CfClusterForwardUBO& ubo, CfAABB* aabbs, cudaStream_t stream)

@@ -188,6 +188,11 @@ cudaError_t launch_one_launch(const FusedCull& f, int warps, int max_lights, uin
 bool cull_config_supported(const CullConfig& c);
 CullConfig default_cull_config(uint32_t clusters, uint32_t lights, uint32_t slices);
 
+// Test knobs of the culling kernels on the current device (cf_device.cuh):
+// the bounded-wait limit and the injected stall bits, per translation unit.
+cudaError_t set_test_knobs_kernels(uint64_t wait_limit_ns, uint32_t inject);
+cudaError_t set_test_knobs_one_launch(uint64_t wait_limit_ns, uint32_t inject);
+
 cudaError_t launch_aabb(const CfClusterForwardUBO& ubo, CfAABB* aabbs, cudaStream_t stream);
 cudaError_t launch_light_xform(const CfLightData* lights, uint32_t count, const float view[16], float4* vlights,
                                uint32_t* nonfinite, cudaStream_t stream);

@@ -11,9 +11,11 @@
 // that uses it is the caller's error.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 
@@ -21,6 +23,7 @@
 #include "cf_kernels.cuh"
 #include "cf_runtime_internal.h"
 #include "cfcull.h"
+#include "cfcull_testing.h"
 
 namespace {
 
@@ -97,6 +100,24 @@ DeviceGuard::~DeviceGuard()
     if (prev_ >= 0) cudaSetDevice(prev_);
 }
 
+namespace {
+std::atomic<int32_t> g_fail_allocation_after{-1};  // allocations to let through before one fails; < 0: none
+}  // namespace
+
+cudaError_t device_malloc(void** ptr, size_t bytes)
+{
+    int32_t n = g_fail_allocation_after.load(std::memory_order_relaxed);
+    while (n >= 0 && !g_fail_allocation_after.compare_exchange_weak(n, n - 1, std::memory_order_relaxed)) {
+    }
+    if (n == 0) {
+        *ptr = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(ptr, bytes);
+}
+
+void set_fail_allocation_after(int32_t n) { g_fail_allocation_after.store(n < 0 ? -1 : n, std::memory_order_relaxed); }
+
 int grow(void** ptr, size_t* capacity, size_t bytes, const char* what)
 {
     if (*capacity >= bytes && *ptr) return CF_SUCCESS;
@@ -108,7 +129,7 @@ int grow(void** ptr, size_t* capacity, size_t bytes, const char* what)
         *capacity = 0;
     }
     if (bytes == 0) return CF_SUCCESS;
-    cudaError_t e = cudaMalloc(ptr, bytes);
+    cudaError_t e = device_malloc(ptr, bytes);
     if (e != cudaSuccess) {
         *ptr = nullptr;
         return cuda_fail(e, what);
@@ -334,7 +355,7 @@ int cf_context_create(int device, CfContext** out)
     CfContext* c = new (std::nothrow) CfContext();
     if (!c) return fail(CF_ERROR_OUT_OF_MEMORY, "host allocation");
     c->device = device;
-    e = cudaMalloc(&c->dev_error, sizeof(uint32_t));
+    e = device_malloc(reinterpret_cast<void**>(&c->dev_error), sizeof(uint32_t));
     if (e != cudaSuccess) {
         delete c;
         return cuda_fail(e, "device error word");
@@ -470,10 +491,10 @@ int cf_resources_cluster_forward_create_buffers(CfResourcesClusterForward* r, ui
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceSynchronize");
     free_cluster_buffers(r);
-    e = cudaMalloc(&r->d_aabbs, (size_t)C * sizeof(CfAABB));
-    if (e == cudaSuccess) e = cudaMalloc(&r->d_cells, (size_t)C * sizeof(CfLightCell));
-    if (e == cudaSuccess) e = cudaMalloc(&r->d_indices, (size_t)C * cap * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&r->d_total, sizeof(uint32_t));
+    e = device_malloc(reinterpret_cast<void**>(&r->d_aabbs), (size_t)C * sizeof(CfAABB));
+    if (e == cudaSuccess) e = device_malloc(reinterpret_cast<void**>(&r->d_cells), (size_t)C * sizeof(CfLightCell));
+    if (e == cudaSuccess) e = device_malloc(reinterpret_cast<void**>(&r->d_indices), (size_t)C * cap * sizeof(uint32_t));
+    if (e == cudaSuccess) e = device_malloc(reinterpret_cast<void**>(&r->d_total), sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(r->d_cells, 0, (size_t)C * sizeof(CfLightCell));
     if (e == cudaSuccess) e = cudaMemset(r->d_total, 0, sizeof(uint32_t));
     if (e != cudaSuccess) {
@@ -590,6 +611,7 @@ int cf_pipeline_aabb_generator_on_window_resized(CfPipelineAABBGenerator* p)
 
 int cf_pipeline_aabb_generator_fill_command_buffer(CfPipelineAABBGenerator* p, void* stream)
 {
+    TraceRange trace("AABB_Generator");
     if (!p) return fail(CF_ERROR_INVALID_ARGUMENT, "null pipeline");
     if (!p->has_ubo) return fail(CF_ERROR_NOT_READY, "SetClusterForwardUBO was never called");
     CfResourcesClusterForward* r = p->res;
@@ -644,7 +666,7 @@ int cf_pipeline_light_culling_enable_work_counters(CfPipelineLightCulling* p, in
         return CF_SUCCESS;
     }
     if (p->d_work) return CF_SUCCESS;
-    cudaError_t e = cudaMalloc(&p->d_work, 2 * sizeof(unsigned long long));
+    cudaError_t e = device_malloc(reinterpret_cast<void**>(&p->d_work), 2 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(p->d_work, 0, 2 * sizeof(unsigned long long));
     return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "work counters");
 }
@@ -708,6 +730,7 @@ int cf_pipeline_light_culling_set_cluster_forward_ubo(CfPipelineLightCulling* p,
 
 int cf_pipeline_light_culling_fill_command_buffer(CfPipelineLightCulling* p, void* stream)
 {
+    TraceRange trace("Light_Culling");
     if (!p) return fail(CF_ERROR_INVALID_ARGUMENT, "null pipeline");
     if (!p->has_ubo) return fail(CF_ERROR_NOT_READY, "SetClusterForwardUBO was never called");
     CfResourcesClusterForward* r = p->res;
@@ -808,6 +831,7 @@ int cf_cull_lights(const CfClusterForwardUBO* ubo, const CfAABB* d_aabbs, const 
                    uint64_t index_capacity, uint32_t* d_total, void* d_workspace, uint64_t workspace_bytes,
                    void* stream)
 {
+    TraceRange trace("Light_Culling");
     if (!ubo || !d_aabbs || !d_cells || !d_indices || !d_workspace || (light_count && !d_lights))
         return fail(CF_ERROR_INVALID_ARGUMENT, "cf_cull_lights: null argument");
     if (light_count > kMaxLights) return fail(CF_ERROR_INVALID_ARGUMENT, "%u lights exceed %u", light_count, kMaxLights);
@@ -827,6 +851,44 @@ int cf_cull_lights(const CfClusterForwardUBO* ubo, const CfAABB* d_aabbs, const 
     unsigned char* ws = static_cast<unsigned char*>(d_workspace);
     return enqueue_cull(*ubo, d_aabbs, d_lights, light_count, cap, d_cells, d_indices, d_total, ws,
                         reinterpret_cast<uint32_t*>(ws), cfg, (cudaStream_t)stream, nullptr);
+}
+
+
+// --- test hooks (include/cfcull_testing.h) ---------------------------------
+namespace {
+std::mutex g_knob_mutex;
+uint64_t g_knob_wait_ns = 0;  // 0: the kernels' default
+uint32_t g_knob_inject = 0;
+
+int apply_test_knobs()
+{
+    const uint64_t limit = g_knob_wait_ns ? g_knob_wait_ns : 2000000000ull;
+    cudaError_t e = cfk::set_test_knobs_kernels(limit, g_knob_inject);
+    if (e == cudaSuccess) e = cfk::set_test_knobs_one_launch(limit, g_knob_inject);
+    return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "set test knobs");
+}
+}  // namespace
+
+int cf_testing_set_wait_limit_ns(uint64_t limit_ns)
+{
+    std::lock_guard<std::mutex> lock(g_knob_mutex);
+    g_knob_wait_ns = limit_ns;
+    return apply_test_knobs();
+}
+
+int cf_testing_inject_stall(uint32_t mode)
+{
+    if (mode & ~(CF_TESTING_STALL_ONE_LAUNCH | CF_TESTING_STALL_BRUTE_FORCE))
+        return fail(CF_ERROR_INVALID_ARGUMENT, "unknown stall injection bits 0x%x", mode);
+    std::lock_guard<std::mutex> lock(g_knob_mutex);
+    g_knob_inject = mode;
+    return apply_test_knobs();
+}
+
+int cf_testing_fail_allocation_after(int32_t n)
+{
+    set_fail_allocation_after(n);
+    return CF_SUCCESS;
 }
 
 }  // extern "C"

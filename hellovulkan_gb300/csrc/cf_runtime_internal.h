@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>  // header-only NVTX v3: a no-op unless a profiler is attached
 #include <stdint.h>
 
 #include "cf_kernels.cuh"
@@ -21,6 +22,18 @@ bool projection_equal(const CfClusterForwardUBO& a, const CfClusterForwardUBO& b
 bool device_addressable(const void* host, void** dev);
 int validate_grid(uint32_t x, uint32_t y, uint32_t z, uint32_t cap, uint32_t* clusters);
 
+// A named NVTX range on the calling host thread for the guard's lifetime, so
+// that the enqueueing of each pass shows in a timeline profiler (nsys, ncu
+// ranges): the counterpart of the reference's Tracy zones ("Light_Culling",
+// PipelineLightCulling.cpp:53; "RecordCommandBuffer", AppBase.cpp:133).
+class TraceRange {
+public:
+    explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange&) = delete;
+    TraceRange& operator=(const TraceRange&) = delete;
+};
+
 // Makes `device` current for the guard's lifetime.
 class DeviceGuard {
 public:
@@ -32,6 +45,9 @@ private:
     int prev_ = -1;
     cudaError_t err_ = cudaSuccess;
 };
+
+// cudaMalloc, except that a test may make it fail (cf_testing_fail_allocation_after).
+cudaError_t device_malloc(void** ptr, size_t bytes);
 
 // Ensures *ptr holds at least `bytes` of zero-filled device memory.
 int grow(void** ptr, size_t* capacity, size_t bytes, const char* what);

@@ -461,6 +461,7 @@ void plan_batch(CfServer* s, int slot_i, const std::vector<Request*>& reqs, Laun
 // its own until the batch's host callback runs).
 int enqueue_batch(CfServer* s, int slot_i, const LaunchPlan& plan, const std::vector<Request*>& reqs)
 {
+    TraceRange trace("Server_Batch");
     StreamSlot& sl = s->slots[slot_i];
     cudaStream_t st = sl.s;
     const uint32_t n = plan.views;
@@ -684,7 +685,7 @@ int cf_server_create(CfContext* ctx, const CfServerConfig* config, CfServer** ou
     s->items_per_slot = c.max_batch_views * c.max_groups_per_view;
     s->t0 = now_s();
     DeviceGuard g(s->device);
-    cudaError_t e = cudaMalloc(&s->d_pool, c.hbm_budget_bytes);
+    cudaError_t e = device_malloc(reinterpret_cast<void**>(&s->d_pool), c.hbm_budget_bytes);
     // The upload stream (light-set copies and jitters) at the highest priority:
     // the batch streams' persistent culling launches fill every SM, and its
     // small kernels must be scheduled ahead of their pending CTAs, or its
@@ -697,8 +698,8 @@ int cf_server_create(CfContext* ctx, const CfServerConfig* config, CfServer** ou
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.s, cudaStreamNonBlocking);
         const size_t tb = table_layout(c.max_batch_views, s->items_per_slot).bytes;
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.upload_fence, cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaMalloc(&sl.d_tables, tb);
-        if (e == cudaSuccess) e = cudaMalloc(&sl.d_queues, cfk::kMaxBatchQueues * sizeof(uint32_t));
+        if (e == cudaSuccess) e = device_malloc(reinterpret_cast<void**>(&sl.d_tables), tb);
+        if (e == cudaSuccess) e = device_malloc(reinterpret_cast<void**>(&sl.d_queues), cfk::kMaxBatchQueues * sizeof(uint32_t));
         if (e == cudaSuccess) e = cudaMallocHost(&sl.h_tables, tb);
     }
     if (e != cudaSuccess) {

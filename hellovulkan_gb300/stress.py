@@ -105,39 +105,37 @@ class StressAnimation:
         return sum(int(np.prod(scenes.STRESS_GRIDS[(i + max(self.epoch, 0)) % 2])) for i in range(self.n_views)) * \
             self.n_lights
 
-    # -- checks ---------------------------------------------------------------
-    def check_view(self, view: int, oracle) -> dict:
-        """Compares view `view`'s lights (against the host restatement of the
-        animation) and its AABBs and culling outputs (against the oracle) at
-        the current frame; returns which parts matched."""
+    # -- state for checking -------------------------------------------------
+    def view_state(self, view: int) -> dict:
+        """View `view` at the current frame, read back to the host: its
+        lights, the orbits it started from, its AABBs, cells and index list,
+        its UBO and cap.  A checker (the tests, the benchmark) compares them
+        with a host restatement; this package only reads them."""
         import torch
-        from oracle import animate_orbits
         torch.cuda.synchronize()
         L = self.n_lights
-        got_lights = self.d_lights[view * L:(view + 1) * L].cpu().numpy()
-        _, pos = animate_orbits(self.h_orbits0[view * L:(view + 1) * L], self.frame_index)
-        lights_ok = bool(np.array_equal(got_lights[:, :4].view(np.uint32), pos.view(np.uint32)))
         pool, s = self.slot(view)
         c = pool["clusters"]
-        aabbs = pool["aabbs"][s].cpu().numpy().reshape(c, 8)
-        cells = pool["cells"][s].cpu().numpy().view(np.uint32).reshape(c, 2)
         total = int(pool["totals"][s].item())
-        idx = pool["indices"][s][:total].cpu().numpy().view(np.uint32)
-        ubo = self.ubos[view]
-        oa = oracle.generate_aabbs(ubo)
-        oc, oi, _ = oracle.cull(ubo, oa, got_lights, self.cap)
-        return {"frame": self.frame_index, "view": view, "lights": lights_ok,
-                "aabbs": bool(np.array_equal(aabbs.view(np.uint32), oa.view(np.uint32))),
-                "cells": bool(np.array_equal(cells, oc)), "indices": bool(np.array_equal(idx, oi))}
+        return {"frame": self.frame_index, "view": view,
+                "lights": self.d_lights[view * L:(view + 1) * L].cpu().numpy(),
+                "orbits0": self.h_orbits0[view * L:(view + 1) * L],
+                "aabbs": pool["aabbs"][s].cpu().numpy().reshape(c, 8),
+                "cells": pool["cells"][s].cpu().numpy().view(np.uint32).reshape(c, 2),
+                "indices": pool["indices"][s][:total].cpu().numpy().view(np.uint32),
+                "ubo": self.ubos[view], "cap": self.cap}
 
     # -- the run --------------------------------------------------------------
-    def run(self, frames: int, stream, check_frames=(), check_views=(), oracle=None, autotune: bool = True) -> dict:
+    def run(self, frames: int, stream, check_frames=(), check_views=(), check=None, autotune: bool = True) -> dict:
         """`frames` frames from frame 0: each frame animates one step, then
         culls every view; a new projection epoch starts every
         frames_per_projection frames.  Every frame is timed with CUDA events on
         `stream`: the frames that start an epoch include the AABB
         regeneration and the capture of the re-planned pass into a CUDA graph;
-        the host-side re-planning before them is timed apart."""
+        the host-side re-planning before them is timed apart.  With `check`
+        (a callable taking view_state(v) and returning a dict of booleans
+        "lights", "aabbs", "cells", "indices"), the views in check_views are
+        checked after the frames in check_frames."""
         import torch
         ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(frames)]
         plan_ms, checks, tests = [], [], 0
@@ -163,9 +161,9 @@ class StressAnimation:
             self.batch.cull(stream)
             ev[f][2].record(stream)
             tests += self.tests_per_frame()
-            if oracle is not None and f in check_frames:
+            if check is not None and f in check_frames:
                 for v in check_views:
-                    checks.append(self.check_view(v, oracle))
+                    checks.append(check(self.view_state(v)))
         torch.cuda.synchronize()
         frame_ms = np.array([a.elapsed_time(c) for a, _, c in ev])
         anim_ms = np.array([a.elapsed_time(b) for a, b, _ in ev])

@@ -134,3 +134,19 @@ def test_scenes_are_seeded_and_shaped():
     mix = scenes.batch_mix(3, n_views=64)
     ls = [v.light_count for v in mix]
     assert min(ls) >= 256 and max(ls) <= 65536 and len({v.grid for v in mix}) == 4
+
+
+@pytest.mark.parametrize("std", ["c11", "c++17"])
+def test_testing_header_compiles_standalone(tmp_path, std):
+    src = tmp_path / ("t.c" if std.startswith("c1") else "t.cpp")
+    src.write_text('#include "cfcull_testing.h"\nint main(void){return CF_TESTING_STALL_ONE_LAUNCH == 1u ? 0 : 1;}\n')
+    cc = "gcc" if std == "c11" else "g++"
+    r = subprocess.run([cc, "-std=" + std, "-Wall", "-Werror", "-I", str(REPO / "include"), str(src), "-o",
+                        str(tmp_path / "a.out")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert subprocess.run([str(tmp_path / "a.out")]).returncode == 0
+
+
+def test_testing_hooks_validate_without_gpu(cflib):
+    assert cflib.cf_testing_inject_stall(0x80) == 1  # unknown bits: CF_ERROR_INVALID_ARGUMENT, no CUDA call
+    assert cflib.cf_testing_fail_allocation_after(3) == 0 and cflib.cf_testing_fail_allocation_after(-1) == 0

@@ -52,7 +52,9 @@ def test_animated_views_match_the_oracle_across_projection_changes(gpu, oracle):
     stream = torch.cuda.Stream()
     # the epoch at frame 5 follows a check (the device is idle), the one at
     # frame 10 follows unchecked frames still queued on the stream
-    rep = st.run(12, stream, check_frames={0, 4, 5, 7, 11}, check_views=(0, 3, 6), oracle=oracle)
+    from bench import check_stress_view
+    rep = st.run(12, stream, check_frames={0, 4, 5, 7, 11}, check_views=(0, 3, 6),
+                 check=lambda state: check_stress_view(state, oracle))
     st.close()
     assert len(rep["checks"]) == 15
     bad = [c for c in rep["checks"] if not all(c[k] for k in ("lights", "aabbs", "cells", "indices"))]

@@ -37,3 +37,40 @@ def test_stress_projections_alternate_grids_and_fov():
     for e in range(3):
         grids = [scenes.STRESS_GRIDS[(i + e) % 2] for i in range(8)]
         assert grids.count((16, 9, 24)) == 4
+
+
+def test_stress_checker_accepts_a_correct_view_and_flags_a_planted_error():
+    """bench.check_stress_view on a view state built on the CPU from the
+    oracle itself: all parts match; a flipped index (planted in the oracle's
+    own output) and a moved light are reported."""
+    from bench import check_stress_view
+    from oracle import Oracle
+    o = Oracle()
+    rng = np.random.default_rng(3)
+    lights0, orbits = scenes.orbit_lights(rng, 1, 300)
+    _, pos = animate_orbits(orbits, 4)
+    lights = lights0.copy()
+    lights[:, 0:4] = pos
+    ubo = scenes.stress_ubo(0, 0, scenes.random_camera(rng))
+    a = o.generate_aabbs(ubo)
+    cells, idx, _ = o.cull(ubo, a, lights, 150)
+    state = {"frame": 4, "view": 0, "lights": lights, "orbits0": orbits, "aabbs": a, "cells": cells,
+             "indices": idx, "ubo": ubo, "cap": 150}
+    assert all(check_stress_view(state, o)[k] for k in ("lights", "aabbs", "cells", "indices"))
+    bad = dict(state, indices=idx.copy())
+    bad["indices"][0] ^= 1
+    assert not check_stress_view(bad, o)["indices"]
+    moved = dict(state, lights=lights.copy())
+    moved["lights"][7, 0] += 1.0
+    r = check_stress_view(moved, o)
+    assert not r["lights"]
+
+
+def test_the_package_never_imports_the_oracle():
+    """The oracle is the checker: nothing under hellovulkan_gb300/ imports it."""
+    import re
+    from pathlib import Path
+    pkg = Path(__file__).resolve().parents[1] / "hellovulkan_gb300"
+    pat = re.compile(r"^\s*(from\s+oracle\b|import\s+oracle\b)", re.M)
+    offenders = [str(p) for p in pkg.rglob("*.py") if pat.search(p.read_text())]
+    assert not offenders, offenders

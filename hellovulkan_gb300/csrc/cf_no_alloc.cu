@@ -13,17 +13,27 @@
 //
 // Limits and rules:
 //  - The array holds kStaticScratchBytes (32 MiB) on every GPU that loads the
-//    library, for as long as the process runs.  A view whose scratch would
-//    not fit is rejected with CF_ERROR_CAPACITY (for example 27 648 clusters
-//    with 16 384 lights and a cap of 150 need about 17 MB and fit).
-//  - The first call on a device looks up the array's device address with
+//    library, for as long as the process runs.  The kernels the automatic
+//    choice picks are used when their scratch fits: a 2560x1600 view of
+//    27 648 clusters with 16 384 lights and a cap of 150 takes the binned
+//    kernels' 31.2 MiB.  Past 32 MiB (that grid with more than about 17 500
+//    lights) the call falls back to the brute-force kernels, whose scratch is
+//    smaller (about 17 MB there) but which run several times slower on such
+//    views (0.36 instead of 0.042 ms at 16 384 lights on a GB300).  A view
+//    whose scratch fits neither way is rejected with CF_ERROR_CAPACITY.
+//  - The first call on a device (and the first after that device's context
+//    was reset) looks up the array's device address with
 //    cudaGetSymbolAddress while that device is current; make that first call
 //    before any stream capture that the call may be part of.
 //  - Every call on a device shares the one array and it keeps the last call's
 //    contents; calls whose kernels overlap on the GPU (different streams, or
 //    threads) race on it and must be serialised by the caller.
+//  - A bounded in-kernel wait that runs out is reported through the caller's
+//    d_device_error word.  Without one the bits go to the array's own word,
+//    which each call clears and nothing reads: pass a word to observe them.
 //  - Nothing here allocates: no cudaMalloc, cudaFree or allocating library
 //    call; the error word is cleared with cudaMemsetAsync.
+#include <cuda.h>  // driver API types only: cuCtxGetId is looked up through the runtime
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -40,9 +50,45 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
 std::mutex g_scratch_mutex;
-unsigned char* g_scratch_ptr[kMaxDevices] = {};
+struct ScratchAddress {
+    unsigned long long context_id = 0;  // the context the address belongs to (0: none yet)
+    unsigned char* ptr = nullptr;
+};
+ScratchAddress g_scratch[kMaxDevices];
 
-// Device address of g_static_scratch on the current device (looked up once per device).
+// Unique ID of the current context (cuCtxGetId, looked up through the
+// runtime so that the driver library need not be linked); 0 if unavailable.
+unsigned long long current_context_id()
+{
+    typedef CUresult (*GetCurrent)(CUcontext*);
+    typedef CUresult (*GetId)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {  // under g_scratch_mutex
+        cudaDriverEntryPointQueryResult q1, q2;
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q2 == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<GetCurrent>(f1);
+            get_id = reinterpret_cast<GetId>(f2);
+        }
+        looked_up = true;
+    }
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
+
+// Device address of g_static_scratch on the current device.  Looked up once
+// per device and context: a context reset (cudaDeviceReset) reloads the
+// module, so a new context ID triggers a new lookup; where no ID can be had
+// the address is looked up on every call.
 int scratch_address(unsigned char** out)
 {
     int dev = 0;
@@ -50,13 +96,16 @@ int scratch_address(unsigned char** out)
     if (e != cudaSuccess) return cfrt::cuda_fail(e, "cudaGetDevice");
     if (dev < 0 || dev >= kMaxDevices) return cfrt::fail(CF_ERROR_UNSUPPORTED, "device ordinal %d out of range", dev);
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_ptr[dev]) {
+    const unsigned long long id = current_context_id();  // 0 before the device's context exists
+    ScratchAddress& c = g_scratch[dev];
+    if (!c.ptr || id == 0 || c.context_id != id) {
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_static_scratch);
+        e = cudaGetSymbolAddress(&p, g_static_scratch);  // also makes the device's context current
         if (e != cudaSuccess) return cfrt::cuda_fail(e, "cudaGetSymbolAddress(static scratch)");
-        g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
+        c.ptr = static_cast<unsigned char*>(p);
+        c.context_id = current_context_id();
     }
-    *out = g_scratch_ptr[dev];
+    *out = c.ptr;
     return CF_SUCCESS;
 }
 

@@ -464,12 +464,17 @@ CFCULL_API int cf_cull_workspace_device_error(void* d_workspace, uint32_t* devic
  * plugin whose device memory its host reserves, a real-time loop that cannot
  * afford cudaMalloc/cudaFree.  Same inputs and outputs as cf_cull_lights, but
  * the scratch comes from a fixed 32 MiB device array that every GPU loading
- * this library holds until the process exits; views needing more scratch are
- * rejected with CF_ERROR_CAPACITY.  The first call on a device looks up that
- * array's address and should come before any stream capture.  All calls on a
- * device share the array: calls that overlap on the GPU race and must be
- * serialised.  d_device_error (optional, device) receives the bounded-wait
- * error bits; without it they go to the array's own word, cleared per call. */
+ * this library holds until the process exits.  A view whose usual kernels
+ * need more scratch than that (a 27 648-cluster grid with more than about
+ * 17 500 lights at a cap of 150) is culled by the brute-force kernels, which
+ * need less but run several times slower on such views; one that fits
+ * neither way is rejected with CF_ERROR_CAPACITY.  The first call on a device
+ * (and the first after its context was reset) looks up that array's address
+ * and should come before any stream capture.  All calls on a device share the
+ * array: calls that overlap on the GPU race and must be serialised.
+ * d_device_error (optional, device) receives the bounded-wait error bits;
+ * without it a timeout cannot be observed (the bits go to the array's own
+ * word, which each call clears). */
 CFCULL_API int cf_cull_lights_static_scratch(const CfClusterForwardUBO* ubo, const CfAABB* d_aabbs,
                                              const CfLightData* d_lights, uint32_t light_count,
                                              uint32_t max_lights_per_cluster, CfLightCell* d_cells,

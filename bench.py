@@ -735,6 +735,38 @@ def measure_stress(ctx, stream, n_views, n_lights, frames, seed=5):
     return rep
 
 
+def run_summary(line: dict) -> dict:
+    """The run's headline figures in one small object (placed last in the
+    JSON line): each measured form of the path with its parity flag."""
+    def pick(d, *keys):
+        for k in keys:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return d
+    e2e = line.get("e2e", {})
+    out = {"plain_large_ms_per_step": line.get("ms_per_step"), "plain_large_parity": line.get("parity_with_oracle"),
+           "e2e_ms_per_frame_pipelined": e2e.get("ms_per_step"), "e2e_ms_one_frame": e2e.get("one_in_flight_ms_per_step"),
+           "roofline_frac": pick(line, "roofline", "frac"),
+           "cpu_baseline_tests_per_s": pick(line, "cpu_baseline", "value"),
+           "plain_small_ms_per_step": pick(line, "plain_small", "ms_per_step"),
+           "plain_small_frac": pick(line, "plain_small", "roofline", "frac"),
+           "plain_small_frac_less_event_floor": pick(line, "plain_small", "roofline_less_event_floor", "frac"),
+           "plain_small_parity": pick(line, "plain_small", "parity_with_oracle"),
+           "batch_views_per_s": pick(line, "batched", "views_per_s"),
+           "batch_speedup_vs_per_view_launch": pick(line, "batched", "speedup_vs_per_view_launch"),
+           "batch_speedup_vs_plain_per_view": pick(line, "batched", "speedup_vs_plain_per_view"),
+           "batch_parity": pick(line, "batched", "parity_sampled_views"),
+           "served_max_sustained_views_per_s": pick(line, "served", "max_sustained_views_per_s"),
+           "served_speedup_vs_plain_per_view": pick(line, "served", "speedup_vs_plain_per_view"),
+           "stress_views_per_s": pick(line, "stress", "views_per_s"), "stress_parity": pick(line, "stress", "parity"),
+           "lookup_unexplained_misses": pick(line, "cluster_lookup", "unexplained_misses"),
+           "frustum_10k_us": pick(line, "frustum_culling", "boxes_10000", "us")}
+    runs = pick(line, "served", "runs") or []
+    out["served_p50_p99_ms"] = {str(int(r["rate"])): [r["latency_p50_ms"], r["latency_p99_ms"]] for r in runs}
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -1021,6 +1053,8 @@ def run_ours(args):
                 "d2h_bytes_per_step": bo, "ms_per_step": 1e3 * e2e_s / e2e_steps, "steps": e2e_steps,
                 "one_in_flight_ms_per_step": 1e3 * e2e_serial_s / e2e_steps,
                 "in_flight": in_flight,
+                "kind": "pipelined throughput with %d frames in flight (a renderer's steady state); the latency of "
+                        "one frame alone is one_in_flight_ms_per_step" % in_flight,
                 "timing": "host clock, pinned host buffers, %d pipelines in flight (step i + %d enqueued before "
                           "the host waits for step i's read-back); one_in_flight: each step waits for its own" % (
                               in_flight, in_flight - 1)},
@@ -1036,6 +1070,7 @@ def run_ours(args):
         "cluster_lookup": lookup,
         "frustum_culling": frustum,
     }
+    line["summary"] = run_summary(line)  # last, so that a record keeping the line's tail keeps it
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()

@@ -39,61 +39,6 @@
 namespace cfk {
 namespace {
 
-// ---- packed float pairs ------------------------------------------------------
-typedef unsigned long long f2;  // two floats in one 64-bit register pair: (lo, hi)
-
-__device__ __forceinline__ f2 f2_pack(float lo, float hi)
-{
-    f2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ void f2_unpack(f2 v, float& lo, float& hi)
-{
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ f2 f2_sub(f2 a, f2 b)
-{
-    f2 r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 f2_mul(f2 a, f2 b)
-{
-    f2 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 f2_add(f2 a, f2 b)
-{
-    f2 r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-
-// hit_fast (cf_device.cuh) for two lights against one box at once: light A
-// in the low halves, light B in the high halves; the box bounds duplicated
-// in both halves.  Each half is exactly hit_fast's arithmetic.
-__device__ __forceinline__ void hit_pair(f2 lx, f2 ly, f2 lz, float ar2, float br2, f2 mnx, f2 mny, f2 mnz, f2 mxx,
-                                         f2 mxy, f2 mxz, bool& ha, bool& hb)
-{
-    float a0, a1, b0, b1;
-    f2_unpack(f2_sub(mnx, lx), a0, a1);
-    f2_unpack(f2_sub(lx, mxx), b0, b1);
-    const f2 dx = f2_pack(max3f(a0, b0, 0.0f), max3f(a1, b1, 0.0f));
-    f2_unpack(f2_sub(mny, ly), a0, a1);
-    f2_unpack(f2_sub(ly, mxy), b0, b1);
-    const f2 dy = f2_pack(max3f(a0, b0, 0.0f), max3f(a1, b1, 0.0f));
-    f2_unpack(f2_sub(mnz, lz), a0, a1);
-    f2_unpack(f2_sub(lz, mxz), b0, b1);
-    const f2 dz = f2_pack(max3f(a0, b0, 0.0f), max3f(a1, b1, 0.0f));
-    const f2 sq = f2_add(f2_add(f2_mul(dx, dx), f2_mul(dy, dy)), f2_mul(dz, dz));
-    float sa, sb;
-    f2_unpack(sq, sa, sb);
-    ha = sa < ar2;
-    hb = sb < br2;
-}
-
 __device__ __forceinline__ void st_relaxed_gpu(unsigned long long* p, unsigned long long v)
 {
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");

@@ -18,7 +18,11 @@ import pytest
 REPO = Path(__file__).resolve().parents[1]
 CSRC = REPO / "hellovulkan_gb300" / "csrc"
 HOST_SOURCES = ["cf_runtime.cpp", "cf_batch.cpp", "cf_server.cpp", "cf_serve_load.cpp"]
-KERNEL_OBJECTS = ["cf_kernels.cu.o", "cf_fused.cu.o", "cf_lookup.cu.o", "cf_frustum.cu.o", "cf_no_alloc.cu.o"]
+
+
+def kernel_objects():
+    """The library's ordinary (not instrumented) objects of every .cu file."""
+    return [REPO / "hellovulkan_gb300" / "_build" / (src.name + ".o") for src in sorted(CSRC.glob("*.cu"))]
 
 
 def cuda_home() -> Path:
@@ -42,7 +46,7 @@ def write_views(path: Path, golden) -> int:
 
 def test_host_code_is_clean_under_address_and_undefined_behaviour_sanitizers(tmp_path, cflib, golden):
     cuda = cuda_home()
-    objs = [REPO / "hellovulkan_gb300" / "_build" / o for o in KERNEL_OBJECTS]
+    objs = kernel_objects()
     if not all(o.exists() for o in objs) or not (cuda / "lib64" / "libcudart_static.a").exists():
         pytest.skip("kernel objects or the static CUDA runtime are not available")
     exe = tmp_path / "sanitize_main"

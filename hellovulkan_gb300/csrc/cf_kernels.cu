@@ -23,7 +23,7 @@
 //   scan_kernel         LightCulling.comp:79-87 with the global atomicAdd replaced
 //   copy_kernel         by an exclusive scan of the group totals in cluster order,
 //   batch_*             then the packed copy of each cluster's hits
-//   jitter_kernel       the served light sets' device jitter
+//   jitter_tasks_kernel the served light sets' device jitters, many sets per launch
 //   orbit_kernel        the animated workload's in-place light motion
 //
 // Floating point follows include/cf_pinned_math.h: every product and sum is an
@@ -1660,11 +1660,11 @@ __device__ __forceinline__ uint64_t splitmix_finalise(uint64_t x)
     return x;
 }
 
-__global__ void __launch_bounds__(256) jitter_kernel(const CfLightData* __restrict__ src, CfLightData* __restrict__ dst,
-                                                     uint32_t n, uint64_t seed, float sigma)
+// Light i of a jitter: its position moved by sigma * (Irwin-Hall variate - 6)
+// per axis, the variate from (seed, i, axis).
+__device__ __forceinline__ void jitter_light(const CfLightData* __restrict__ src, CfLightData* __restrict__ dst,
+                                             uint32_t i, uint64_t seed, float sigma)
 {
-    const uint32_t i = blockIdx.x * 256 + threadIdx.x;
-    if (i >= n) return;
     CfLightData L = src[i];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -1677,6 +1677,27 @@ __global__ void __launch_bounds__(256) jitter_kernel(const CfLightData* __restri
         L.position[a] = __fadd_rn(L.position[a], __fmul_rn(sigma, __fsub_rn(s, 6.0f)));
     }
     dst[i] = L;
+}
+
+// Many jitters in one launch: block b belongs to task j where
+// block_start[j] <= b < block_start[j + 1].
+struct JitterTaskTable {
+    JitterTask t[kMaxJitterTasks];
+    uint32_t block_start[kMaxJitterTasks + 1];
+    uint32_t count;
+};
+
+__global__ void __launch_bounds__(256) jitter_tasks_kernel(const JitterTaskTable T)
+{
+    uint32_t lo = 0, hi = T.count;  // block_start[lo] <= blockIdx.x < block_start[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (T.block_start[mid] <= blockIdx.x) lo = mid;
+        else hi = mid;
+    }
+    const JitterTask& t = T.t[lo];
+    const uint32_t i = (blockIdx.x - T.block_start[lo]) * 256 + threadIdx.x;
+    if (i < t.n) jitter_light(t.src, t.dst, i, t.seed, t.sigma);
 }
 
 // Moves each light `frames` steps along its orbit (CfLightOrbit), in place:
@@ -1707,12 +1728,30 @@ __global__ void __launch_bounds__(256) orbit_kernel(CfLightData* __restrict__ li
 
 }  // namespace
 
-cudaError_t launch_jitter(const CfLightData* src, CfLightData* dst, uint32_t n, uint64_t seed, float sigma,
-                          cudaStream_t stream)
+cudaError_t launch_jitter_tasks(const JitterTask* tasks, uint32_t n, cudaStream_t stream)
 {
-    if (n == 0) return cudaSuccess;
-    jitter_kernel<<<(n + 255) / 256, 256, 0, stream>>>(src, dst, n, seed, sigma);
-    return cudaGetLastError();
+    for (uint32_t first = 0; first < n;) {
+        JitterTaskTable T{};
+        uint32_t blocks = 0;
+        T.count = 0;
+        // a task that reads what an earlier task of this launch writes goes into the next launch
+        while (first + T.count < n && T.count < kMaxJitterTasks) {
+            const JitterTask& t = tasks[first + T.count];
+            bool reads_earlier = false;
+            for (uint32_t q = 0; q < T.count; ++q) reads_earlier |= T.t[q].dst == t.src;
+            if (reads_earlier) break;
+            T.t[T.count] = t;
+            T.block_start[T.count] = blocks;
+            blocks += (t.n + 255) / 256;
+            ++T.count;
+        }
+        T.block_start[T.count] = blocks;
+        if (blocks) jitter_tasks_kernel<<<blocks, 256, 0, stream>>>(T);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        first += T.count;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_orbits(CfLightData* lights, CfLightOrbit* orbits, uint64_t n, uint32_t frames, cudaStream_t stream)

@@ -203,9 +203,19 @@ cudaError_t launch_finalize(const ViewCull& v, cudaStream_t stream);
 cudaError_t launch_readback(const CfLightCell* cells, uint32_t clusters, const uint32_t* indices,
                             const uint32_t* d_total, uint64_t capacity, CfLightCell* h_cells, uint32_t* h_indices,
                             uint32_t* h_total, cudaStream_t stream);
-// dst = src with positions moved by sigma * (Irwin-Hall variate) from (seed, light, axis).
-cudaError_t launch_jitter(const CfLightData* src, CfLightData* dst, uint32_t n, uint64_t seed, float sigma,
-                          cudaStream_t stream);
+// Jitters of many light sets in as few launches as possible (one per run of
+// tasks none of which reads another's output), in task order: each task's
+// dst = src with positions moved by sigma * (Irwin-Hall variate) from (seed,
+// light, axis).
+struct JitterTask {
+    const CfLightData* src;
+    CfLightData* dst;
+    uint64_t seed;
+    uint32_t n;
+    float sigma;
+};
+constexpr uint32_t kMaxJitterTasks = 32;  // tasks per launch (passed by value)
+cudaError_t launch_jitter_tasks(const JitterTask* tasks, uint32_t n, cudaStream_t stream);
 // Every light `frames` steps along its orbit, in place (CfLightOrbit).
 cudaError_t launch_orbits(CfLightData* lights, CfLightOrbit* orbits, uint64_t n, uint32_t frames, cudaStream_t stream);
 

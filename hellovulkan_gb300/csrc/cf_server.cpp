@@ -63,6 +63,16 @@ struct LightVersion {
     bool retired = false;
 };
 
+// A jitter waiting for the worker: it reads `src` and writes `dst` (both
+// held by a reference until the launch is enqueued, after which the upload
+// stream's order protects them like any fill).
+struct JitterJob {
+    LightVersion* src;
+    LightVersion* dst;
+    uint64_t seed;
+    float sigma;
+};
+
 struct LightSet {
     LightVersion* cur = nullptr;
     uint64_t last_use = 0;
@@ -171,6 +181,7 @@ struct CfServer {
     std::mutex mu;
     std::condition_variable cv, done_cv;
     std::deque<Request*> pending;
+    std::vector<JitterJob> jitters;  // queued by cf_server_jitter_light_set, launched before the next batch
     std::vector<StreamSlot> slots;
     std::map<uint64_t, LightSet> sets;
     std::vector<AabbEntry*> aabbs;
@@ -529,6 +540,30 @@ void finish_batch(CfServer* s, Batch* b)
     delete b;
 }
 
+// Launches queued jitters on the upload stream (no lock held), in queue order.
+int launch_jitters(CfServer* s, const std::vector<JitterJob>& jobs)
+{
+    if (jobs.empty()) return CF_SUCCESS;
+    std::vector<cfk::JitterTask> tasks(jobs.size());
+    for (size_t i = 0; i < jobs.size(); ++i)
+        tasks[i] = cfk::JitterTask{reinterpret_cast<const CfLightData*>(jobs[i].src->d),
+                                   reinterpret_cast<CfLightData*>(jobs[i].dst->d), jobs[i].seed, jobs[i].src->count,
+                                   jobs[i].sigma};
+    const cudaError_t e = cfk::launch_jitter_tasks(tasks.data(), (uint32_t)tasks.size(), s->upload);
+    return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "light set jitters");
+}
+
+// Drops the jobs' holds on their versions (lock held).
+void release_jitters(CfServer* s, const std::vector<JitterJob>& jobs)
+{
+    for (const JitterJob& j : jobs) {
+        j.src->refs--;
+        j.dst->refs--;
+        free_version_if_dead(s, j.src);
+        free_version_if_dead(s, j.dst);
+    }
+}
+
 void worker_main(CfServer* s)
 {
     DeviceGuard g(s->device);
@@ -582,11 +617,16 @@ void worker_main(CfServer* s)
             s->slots[q].busy = true;
             const double t_launch = now_s();
             for (Request* r : batch) r->t_launch = t_launch;
-            // The CUDA calls go without the lock, so that submitters, pollers
-            // and uploads are not held up behind them.
+            // The jitters queued so far go first, on the upload stream, ahead of
+            // the fence the batch waits on.  The CUDA calls go without the lock,
+            // so that submitters, pollers and uploads are not held up behind them.
+            std::vector<JitterJob> jobs;
+            jobs.swap(s->jitters);
             lk.unlock();
-            const int st = enqueue_batch(s, (int)q, plan, batch);
+            int st = launch_jitters(s, jobs);
+            if (st == CF_SUCCESS) st = enqueue_batch(s, (int)q, plan, batch);
             lk.lock();
+            release_jitters(s, jobs);
             if (st != CF_SUCCESS) {
                 s->slots[q].busy = false;
                 for (AabbEntry* a : plan.generate) a->generated = false;
@@ -603,6 +643,23 @@ void worker_main(CfServer* s)
                 s->stats.views_launched += batch.size();
                 s->stats.max_batch_views = std::max<uint32_t>(s->stats.max_batch_views, (uint32_t)batch.size());
                 launched = true;
+            }
+        }
+        if (!launched && !s->jitters.empty()) {
+            // No batch went out to carry them: launch the queued jitters alone,
+            // so that their versions do not hold arena memory while idle.  If
+            // the launch fails they go back to the queue, and the next batch
+            // retries them and reports the failure to its requests.
+            std::vector<JitterJob> jobs;
+            jobs.swap(s->jitters);
+            lk.unlock();
+            const int st = launch_jitters(s, jobs);
+            lk.lock();
+            if (st == CF_SUCCESS) {
+                release_jitters(s, jobs);
+            } else {
+                jobs.insert(jobs.end(), s->jitters.begin(), s->jitters.end());
+                s->jitters.swap(jobs);
             }
         }
         const bool busy = std::any_of(s->slots.begin(), s->slots.end(), [](const StreamSlot& x) { return x.busy; });
@@ -726,6 +783,8 @@ int cf_server_destroy(CfServer* s)
     if (s->worker.joinable()) s->worker.join();
     DeviceGuard g(s->device);
     cudaDeviceSynchronize();
+    release_jitters(s, s->jitters);  // never launched: nothing will read their versions
+    s->jitters.clear();
     for (auto& kv : s->holding) delete kv.second;
     for (auto& kv : s->sets) delete kv.second.cur;
     for (AabbEntry* a : s->aabbs) {
@@ -812,38 +871,26 @@ int cf_server_update_light_set(CfServer* s, uint64_t id, const CfLightData* ligh
 int cf_server_jitter_light_set(CfServer* s, uint64_t id, uint64_t seed, float sigma)
 {
     if (!s) return fail(CF_ERROR_INVALID_ARGUMENT, "null server");
-    LightVersion *v = nullptr, *old = nullptr;
-    {
-        std::lock_guard<std::mutex> lk(s->mu);
-        auto it = s->sets.find(id);
-        if (it == s->sets.end()) return fail(CF_ERROR_NOT_READY, "light set %llu is not resident", (unsigned long long)id);
-        old = it->second.cur;
-        old->refs++;  // neither evictable nor freed while the jitter reads it
-        v = new (std::nothrow) LightVersion();
-        unsigned char* d = v ? arena_alloc(s, std::max<size_t>((size_t)old->count * sizeof(CfLightData), 256)) : nullptr;
-        if (!v || !d) {
-            delete v;
-            old->refs--;
-            return fail(CF_ERROR_BUDGET, "no room for a new version of light set %llu", (unsigned long long)id);
-        }
-        v->d = d;
-        v->count = old->count;
-    }
-    cudaError_t e;
-    {
-        // Not under `mu`.  The fill of `old` was enqueued on the upload stream
-        // before `old` was published, so this jitter runs after it.
-        DeviceGuard g(s->device);
-        e = cfk::launch_jitter(reinterpret_cast<const CfLightData*>(old->d), reinterpret_cast<CfLightData*>(v->d),
-                               old->count, seed, sigma, s->upload);
-    }
     std::lock_guard<std::mutex> lk(s->mu);
-    if (e != cudaSuccess) {
-        old->refs--;
-        free_version_if_dead(s, old);
-        drop_unpublished(s, v);
-        return cuda_fail(e, "light set jitter");
+    auto it = s->sets.find(id);
+    if (it == s->sets.end()) return fail(CF_ERROR_NOT_READY, "light set %llu is not resident", (unsigned long long)id);
+    LightVersion* old = it->second.cur;
+    old->refs += 2;  // one for the queued jitter, one that publish_version releases; neither evictable meanwhile
+    LightVersion* v = new (std::nothrow) LightVersion();
+    unsigned char* d = v ? arena_alloc(s, std::max<size_t>((size_t)old->count * sizeof(CfLightData), 256)) : nullptr;
+    if (!v || !d) {
+        delete v;
+        old->refs -= 2;
+        return fail(CF_ERROR_BUDGET, "no room for a new version of light set %llu", (unsigned long long)id);
     }
+    v->d = d;
+    v->count = old->count;
+    // The jitter itself is queued: the worker launches every queued jitter on
+    // the upload stream in one go before the next batch's upload fence, so a
+    // request that binds the new version reads it only after it is written,
+    // and the caller pays no CUDA call here.
+    v->refs++;
+    s->jitters.push_back(JitterJob{old, v, seed, sigma});
     return publish_version(s, id, v, old);
 }
 

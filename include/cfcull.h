@@ -327,7 +327,11 @@ CFCULL_API int cf_server_update_light_set(CfServer* server, uint64_t id, const C
  * position += sigma * (s - 6), s the sum of 12 uniforms in [0, 1) drawn from
  * a splitmix64 hash of (seed + light * 0x9E3779B97F4A7C15 + (axis * 12 + term)
  * * 0xD1B54A32D192ED03), u = (hash >> 40) * 2^-24, every operation rounded
- * to nearest in that order, so a host can reproduce the result bit for bit. */
+ * to nearest in that order, so a host can reproduce the result bit for bit.
+ * The call makes no CUDA call: the server's worker launches every queued
+ * jitter (up to 32 sets per launch) on the upload stream ahead of the next
+ * batch's upload fence, or alone when no batch is ready, so every request that
+ * binds the new version reads it after it is written. */
 CFCULL_API int cf_server_jitter_light_set(CfServer* server, uint64_t id, uint64_t seed, float sigma);
 CFCULL_API int cf_server_release_light_set(CfServer* server, uint64_t id);
 CFCULL_API int cf_server_is_light_set_resident(CfServer* server, uint64_t id, int* resident);

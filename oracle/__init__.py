@@ -229,7 +229,7 @@ class Reference:
 
 def jitter_lights(lights: np.ndarray, seed: int, sigma: float) -> np.ndarray:
     """Host restatement of the server's light jitter (cf_server_jitter_light_set,
-    hellovulkan_gb300/csrc/cf_kernels.cu jitter_kernel), bit for bit."""
+    hellovulkan_gb300/csrc/cf_kernels.cu jitter_light), bit for bit."""
     L = np.array(lights, np.float32, copy=True).reshape(-1, 12)
     n = L.shape[0]
     i = np.arange(n, dtype=np.uint64)

@@ -135,3 +135,46 @@ def test_load_driver_completes_every_request(gpu):
     assert rep["latency_p50_ms"] > 0 and rep["latency_p99_ms"] >= rep["latency_p50_ms"]
     assert rep["reused_sets"] > 0 and rep["new_sets"] > 0
     srv.close()
+
+
+def test_queued_jitters_chains_releases_and_idle_flush(gpu, oracle):
+    """Jitters wait in the server's queue until the worker launches them (up
+    to 32 sets per launch, a set whose source another queued jitter writes in
+    a later launch): 40 sets jittered at once, one set jittered three times
+    with a request after each step, a set released while its jitter waits,
+    and a jitter flushed with no batch to carry it.  Every result matches the
+    oracle on the host restatement of the jitter chain."""
+    import time
+
+    from hellovulkan_gb300.server import Server
+    from oracle import jitter_lights
+    srv = Server(gpu, budget_bytes=1 << 30, max_batch_views=16, streams=2)
+    rng = np.random.default_rng(5)
+    v = scenes.plain_small(4)
+    sets = [scenes.uniform_box_lights(rng, int(n), [-20, -10, -60], [20, 10, -1], 1.0, 6.0)
+            for n in rng.integers(1, 700, 40)]
+    ids = [srv.register(s) for s in sets]
+    expect = {}
+    for k, (sid, s) in enumerate(zip(ids, sets)):
+        srv.jitter(sid, 100 + k, 0.5)
+        expect[srv.submit(v.ubo, sid)] = jitter_lights(s, 100 + k, 0.5)
+    chain = jitter_lights(sets[0], 100, 0.5)  # set 0 again: each step reads the previous step's version
+    for step in range(3):
+        srv.jitter(ids[0], 7 + step, 0.25)
+        chain = jitter_lights(chain, 7 + step, 0.25)
+        expect[srv.submit(v.ubo, ids[0])] = chain
+    gone = srv.register(sets[1])
+    srv.jitter(gone, 99, 0.5)
+    srv.release_set(gone)  # its queued jitter still holds both versions until launched
+    extra = srv.register(sets[2])
+    srv.jitter(extra, 55, 0.5)
+    time.sleep(0.05)  # no request: the worker flushes the jitter alone
+    expect[srv.submit(v.ubo, extra)] = jitter_lights(sets[2], 55, 0.5)
+    done = take(srv, len(expect))
+    for rid, lights in expect.items():
+        assert done[rid].status == 0
+        cells, idx = srv.read(done[rid])
+        oc, oi = oracle_result(oracle, v.ubo, lights)
+        assert np.array_equal(cells, oc) and np.array_equal(idx, oi), rid
+        srv.release(rid)
+    srv.close()

@@ -24,6 +24,7 @@
 //   copy_kernel         by an exclusive scan of the group totals in cluster order,
 //   batch_*             then the packed copy of each cluster's hits
 //   jitter_tasks_kernel the served light sets' device jitters, many sets per launch
+//   upload_tasks_kernel the served light sets' copies from pinned host memory, many per launch
 //   orbit_kernel        the animated workload's in-place light motion
 //
 // Floating point follows include/cf_pinned_math.h: every product and sum is an
@@ -1700,6 +1701,36 @@ __global__ void __launch_bounds__(256) jitter_tasks_kernel(const JitterTaskTable
     if (i < t.n) jitter_light(t.src, t.dst, i, t.seed, t.sigma);
 }
 
+// Copies of many light sets from device-mapped pinned host memory in one
+// launch: block b belongs to task j where block_start[j] <= b <
+// block_start[j + 1] and copies 16-byte words [256*4*(b - block_start[j]),
+// +1024) of it, four loads in flight per thread (the reads cross the
+// host link, so the latency is hidden by loads in flight, not by occupancy).
+struct UploadTaskTable {
+    UploadTask t[kMaxUploadTasks];
+    uint32_t block_start[kMaxUploadTasks + 1];
+    uint32_t count;
+};
+
+__global__ void __launch_bounds__(256) upload_tasks_kernel(const UploadTaskTable T)
+{
+    uint32_t lo = 0, hi = T.count;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (T.block_start[mid] <= blockIdx.x) lo = mid;
+        else hi = mid;
+    }
+    const UploadTask& t = T.t[lo];
+    const uint32_t base = (blockIdx.x - T.block_start[lo]) * 1024 + threadIdx.x;
+    uint4 w[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (base + k * 256 < t.words) w[k] = t.src[base + k * 256];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (base + k * 256 < t.words) t.dst[base + k * 256] = w[k];
+}
+
 // Moves each light `frames` steps along its orbit (CfLightOrbit), in place:
 // per step x' = c*x - s*z, z' = s*x + c*z (products, then the difference or
 // sum, each rounded to nearest), then position = center + (x', 0, z').  Reads
@@ -1747,6 +1778,28 @@ cudaError_t launch_jitter_tasks(const JitterTask* tasks, uint32_t n, cudaStream_
         }
         T.block_start[T.count] = blocks;
         if (blocks) jitter_tasks_kernel<<<blocks, 256, 0, stream>>>(T);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        first += T.count;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_upload_tasks(const UploadTask* tasks, uint32_t n, cudaStream_t stream)
+{
+    for (uint32_t first = 0; first < n;) {
+        UploadTaskTable T{};
+        uint32_t blocks = 0;
+        T.count = 0;
+        while (first + T.count < n && T.count < kMaxUploadTasks) {
+            const UploadTask& t = tasks[first + T.count];
+            T.t[T.count] = t;
+            T.block_start[T.count] = blocks;
+            blocks += (uint32_t)((t.words + 1023) / 1024);
+            ++T.count;
+        }
+        T.block_start[T.count] = blocks;
+        if (blocks) upload_tasks_kernel<<<blocks, 256, 0, stream>>>(T);
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         first += T.count;

@@ -216,6 +216,15 @@ struct JitterTask {
 };
 constexpr uint32_t kMaxJitterTasks = 32;  // tasks per launch (passed by value)
 cudaError_t launch_jitter_tasks(const JitterTask* tasks, uint32_t n, cudaStream_t stream);
+// Copies of many buffers from device-mapped pinned host memory (16-byte
+// aligned, whole 16-byte words) in as few launches as possible.
+struct UploadTask {
+    const uint4* src;  // the host buffer's device-side address
+    uint4* dst;
+    uint32_t words;    // 16-byte words
+};
+constexpr uint32_t kMaxUploadTasks = 48;  // tasks per launch (passed by value)
+cudaError_t launch_upload_tasks(const UploadTask* tasks, uint32_t n, cudaStream_t stream);
 // Every light `frames` steps along its orbit, in place (CfLightOrbit).
 cudaError_t launch_orbits(CfLightData* lights, CfLightOrbit* orbits, uint64_t n, uint32_t frames, cudaStream_t stream);
 

@@ -63,12 +63,16 @@ struct LightVersion {
     bool retired = false;
 };
 
-// A jitter waiting for the worker: it reads `src` and writes `dst` (both
-// held by a reference until the launch is enqueued, after which the upload
-// stream's order protects them like any fill).
-struct JitterJob {
-    LightVersion* src;
+// Work that writes a new version, waiting for the worker: a jitter of `src`,
+// or (src null) a copy from `host`, pinned host memory the device reads
+// directly.  Both versions are held by a reference until the launch is
+// enqueued, after which the upload stream's order protects them like any
+// fill.  `host` must stay unchanged until the first request that uses the
+// version has completed, as for a copy from pinned memory.
+struct VersionJob {
     LightVersion* dst;
+    LightVersion* src;
+    const void* host;
     uint64_t seed;
     float sigma;
 };
@@ -181,7 +185,7 @@ struct CfServer {
     std::mutex mu;
     std::condition_variable cv, done_cv;
     std::deque<Request*> pending;
-    std::vector<JitterJob> jitters;  // queued by cf_server_jitter_light_set, launched before the next batch
+    std::vector<VersionJob> jobs;  // queued uploads and jitters, launched before the next batch
     std::vector<StreamSlot> slots;
     std::map<uint64_t, LightSet> sets;
     std::vector<AabbEntry*> aabbs;
@@ -540,27 +544,38 @@ void finish_batch(CfServer* s, Batch* b)
     delete b;
 }
 
-// Launches queued jitters on the upload stream (no lock held), in queue order.
-int launch_jitters(CfServer* s, const std::vector<JitterJob>& jobs)
+// Launches queued version jobs on the upload stream (no lock held): every
+// upload, then every jitter in queue order.  Running the uploads first is
+// safe: an upload writes fresh memory that no queued jitter writes or reads
+// except as its source, and that makes it a dependency, never the reverse.
+int launch_jobs(CfServer* s, const std::vector<VersionJob>& jobs)
 {
     if (jobs.empty()) return CF_SUCCESS;
-    std::vector<cfk::JitterTask> tasks(jobs.size());
-    for (size_t i = 0; i < jobs.size(); ++i)
-        tasks[i] = cfk::JitterTask{reinterpret_cast<const CfLightData*>(jobs[i].src->d),
-                                   reinterpret_cast<CfLightData*>(jobs[i].dst->d), jobs[i].seed, jobs[i].src->count,
-                                   jobs[i].sigma};
-    const cudaError_t e = cfk::launch_jitter_tasks(tasks.data(), (uint32_t)tasks.size(), s->upload);
-    return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "light set jitters");
+    std::vector<cfk::UploadTask> uploads;
+    std::vector<cfk::JitterTask> jitters;
+    for (const VersionJob& j : jobs) {
+        if (j.src)
+            jitters.push_back(cfk::JitterTask{reinterpret_cast<const CfLightData*>(j.src->d),
+                                              reinterpret_cast<CfLightData*>(j.dst->d), j.seed, j.src->count, j.sigma});
+        else
+            uploads.push_back(cfk::UploadTask{static_cast<const uint4*>(j.host), reinterpret_cast<uint4*>(j.dst->d),
+                                              (uint32_t)((size_t)j.dst->count * sizeof(CfLightData) / 16)});
+    }
+    cudaError_t e = cfk::launch_upload_tasks(uploads.data(), (uint32_t)uploads.size(), s->upload);
+    if (e == cudaSuccess) e = cfk::launch_jitter_tasks(jitters.data(), (uint32_t)jitters.size(), s->upload);
+    return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "light set uploads and jitters");
 }
 
 // Drops the jobs' holds on their versions (lock held).
-void release_jitters(CfServer* s, const std::vector<JitterJob>& jobs)
+void release_jobs(CfServer* s, const std::vector<VersionJob>& jobs)
 {
-    for (const JitterJob& j : jobs) {
-        j.src->refs--;
+    for (const VersionJob& j : jobs) {
         j.dst->refs--;
-        free_version_if_dead(s, j.src);
         free_version_if_dead(s, j.dst);
+        if (j.src) {
+            j.src->refs--;
+            free_version_if_dead(s, j.src);
+        }
     }
 }
 
@@ -617,16 +632,17 @@ void worker_main(CfServer* s)
             s->slots[q].busy = true;
             const double t_launch = now_s();
             for (Request* r : batch) r->t_launch = t_launch;
-            // The jitters queued so far go first, on the upload stream, ahead of
-            // the fence the batch waits on.  The CUDA calls go without the lock,
-            // so that submitters, pollers and uploads are not held up behind them.
-            std::vector<JitterJob> jobs;
-            jobs.swap(s->jitters);
+            // The uploads and jitters queued so far go first, on the upload
+            // stream, ahead of the fence the batch waits on.  The CUDA calls go
+            // without the lock, so that submitters, pollers and uploads are not
+            // held up behind them.
+            std::vector<VersionJob> jobs;
+            jobs.swap(s->jobs);
             lk.unlock();
-            int st = launch_jitters(s, jobs);
+            int st = launch_jobs(s, jobs);
             if (st == CF_SUCCESS) st = enqueue_batch(s, (int)q, plan, batch);
             lk.lock();
-            release_jitters(s, jobs);
+            release_jobs(s, jobs);
             if (st != CF_SUCCESS) {
                 s->slots[q].busy = false;
                 for (AabbEntry* a : plan.generate) a->generated = false;
@@ -645,21 +661,22 @@ void worker_main(CfServer* s)
                 launched = true;
             }
         }
-        if (!launched && !s->jitters.empty()) {
-            // No batch went out to carry them: launch the queued jitters alone,
-            // so that their versions do not hold arena memory while idle.  If
-            // the launch fails they go back to the queue, and the next batch
-            // retries them and reports the failure to its requests.
-            std::vector<JitterJob> jobs;
-            jobs.swap(s->jitters);
+        if (!launched && !s->jobs.empty()) {
+            // No batch went out to carry them: launch the queued jobs alone, so
+            // that their versions do not hold arena memory (nor their callers'
+            // host buffers) while idle.  If the launch fails they go back to the
+            // queue, and the next batch retries them and reports the failure to
+            // its requests.
+            std::vector<VersionJob> jobs;
+            jobs.swap(s->jobs);
             lk.unlock();
-            const int st = launch_jitters(s, jobs);
+            const int st = launch_jobs(s, jobs);
             lk.lock();
             if (st == CF_SUCCESS) {
-                release_jitters(s, jobs);
+                release_jobs(s, jobs);
             } else {
-                jobs.insert(jobs.end(), s->jitters.begin(), s->jitters.end());
-                s->jitters.swap(jobs);
+                jobs.insert(jobs.end(), s->jobs.begin(), s->jobs.end());
+                s->jobs.swap(jobs);
             }
         }
         const bool busy = std::any_of(s->slots.begin(), s->slots.end(), [](const StreamSlot& x) { return x.busy; });
@@ -687,6 +704,22 @@ int upload_version(CfServer* s, const CfLightData* host, uint32_t n, LightVersio
     (void)host;
     *out = v;
     return CF_SUCCESS;
+}
+
+// The device-side address of `host` when it lies in pinned host memory the
+// device can read directly (16-byte aligned), else null: pageable memory is
+// copied at once by fill_from_host, since its caller may reuse it on return.
+const void* device_view_of_pinned(CfServer* s, const void* host)
+{
+    DeviceGuard g(s->device);
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();  // clear it: an unknown pointer is simply not pinned
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer || (reinterpret_cast<uintptr_t>(a.devicePointer) & 15u))
+        return nullptr;
+    return a.devicePointer;
 }
 
 // Enqueues the copy that fills v on the upload stream.  Called WITHOUT `mu`:
@@ -783,8 +816,8 @@ int cf_server_destroy(CfServer* s)
     if (s->worker.joinable()) s->worker.join();
     DeviceGuard g(s->device);
     cudaDeviceSynchronize();
-    release_jitters(s, s->jitters);  // never launched: nothing will read their versions
-    s->jitters.clear();
+    release_jobs(s, s->jobs);  // never launched: nothing will read their versions
+    s->jobs.clear();
     for (auto& kv : s->holding) delete kv.second;
     for (auto& kv : s->sets) delete kv.second.cur;
     for (AabbEntry* a : s->aabbs) {
@@ -802,11 +835,20 @@ int cf_server_register_light_set(CfServer* s, const CfLightData* lights, uint32_
 {
     if (!s || !id || (count && !lights)) return fail(CF_ERROR_INVALID_ARGUMENT, "null argument");
     if (count > kMaxLights) return fail(CF_ERROR_INVALID_ARGUMENT, "too many lights");
+    const void* mapped = count ? device_view_of_pinned(s, lights) : nullptr;
     LightVersion* v = nullptr;
     {
         std::lock_guard<std::mutex> lk(s->mu);
         const int st = upload_version(s, lights, count, &v);
         if (st) return st;
+        if (mapped) {  // the worker copies it, with the other queued jobs
+            v->refs++;
+            s->jobs.push_back(VersionJob{v, nullptr, mapped, 0, 0.0f});
+            const uint64_t sid = s->next_set++;
+            s->sets[sid] = LightSet{v, ++s->tick};
+            *id = sid;
+            return CF_SUCCESS;
+        }
     }
     const int st = fill_from_host(s, v, lights);  // not under `mu`
     std::lock_guard<std::mutex> lk(s->mu);
@@ -844,6 +886,7 @@ int publish_version(CfServer* s, uint64_t id, LightVersion* v, LightVersion* pin
 int cf_server_update_light_set(CfServer* s, uint64_t id, const CfLightData* lights, uint32_t count)
 {
     if (!s || (count && !lights)) return fail(CF_ERROR_INVALID_ARGUMENT, "null argument");
+    const void* mapped = count ? device_view_of_pinned(s, lights) : nullptr;
     LightVersion *v = nullptr, *old = nullptr;
     {
         std::lock_guard<std::mutex> lk(s->mu);
@@ -855,6 +898,11 @@ int cf_server_update_light_set(CfServer* s, uint64_t id, const CfLightData* ligh
         if (st) {
             old->refs--;
             return st;
+        }
+        if (mapped) {  // the worker copies it, with the other queued jobs
+            v->refs++;
+            s->jobs.push_back(VersionJob{v, nullptr, mapped, 0, 0.0f});
+            return publish_version(s, id, v, old);
         }
     }
     const int st = fill_from_host(s, v, lights);  // not under `mu`
@@ -885,12 +933,12 @@ int cf_server_jitter_light_set(CfServer* s, uint64_t id, uint64_t seed, float si
     }
     v->d = d;
     v->count = old->count;
-    // The jitter itself is queued: the worker launches every queued jitter on
-    // the upload stream in one go before the next batch's upload fence, so a
+    // The jitter itself is queued: the worker launches the queued jobs on the
+    // upload stream in one go before the next batch's upload fence, so a
     // request that binds the new version reads it only after it is written,
     // and the caller pays no CUDA call here.
     v->refs++;
-    s->jitters.push_back(JitterJob{old, v, seed, sigma});
+    s->jobs.push_back(VersionJob{v, old, nullptr, seed, sigma});
     return publish_version(s, id, v, old);
 }
 

@@ -27,6 +27,11 @@ class Server:
         self.handle = h
 
     def register(self, lights: np.ndarray) -> int:
+        """A new resident light set.  From pageable memory the lights are
+        copied before the call returns; from pinned memory (a pinned tensor's
+        numpy view) the server's worker copies them before the next batch, so
+        the array must stay alive and unchanged until the first request that
+        uses the set has completed."""
         a = np.ascontiguousarray(lights, np.float32).reshape(-1, 12)
         out = C.c_uint64()
         check(lib().cf_server_register_light_set(self.handle, a.ctypes.data if a.size else None, a.shape[0],
@@ -34,6 +39,8 @@ class Server:
         return int(out.value)
 
     def update(self, set_id: int, lights: np.ndarray) -> None:
+        """A new version of a set for requests submitted from now on (the
+        same rule on pinned memory as register)."""
         a = np.ascontiguousarray(lights, np.float32).reshape(-1, 12)
         check(lib().cf_server_update_light_set(self.handle, set_id, a.ctypes.data if a.size else None, a.shape[0]))
 
@@ -134,6 +141,9 @@ def run_load(server: Server, rate: float, duration: float, seed: int = 4, base_s
     pinned = _pin(base_sets)
     if pinned is not None:
         base_sets = [t.numpy() for t in pinned]
+        # the server may still copy from them after the run (a set registered
+        # by a request that failed is copied when the worker is next idle)
+        server._keep_alive = getattr(server, "_keep_alive", []) + [pinned]
     projs = (CfClusterForwardUBO * 4)(*projection_ubos())
     ptrs = (C.c_void_p * len(base_sets))(*[b.ctypes.data for b in base_sets])
     counts = (C.c_uint32 * len(base_sets))(*[b.shape[0] for b in base_sets])

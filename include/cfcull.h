@@ -315,10 +315,14 @@ CFCULL_API int cf_server_destroy(CfServer* server);
  * cannot fit).  Sets no submitted request uses are evicted least recently
  * used when admission needs room; submitting against an evicted set returns
  * CF_ERROR_NOT_READY (register it again).  The copy follows cudaMemcpyAsync's
- * rule: from pageable memory `lights` is free to reuse when the call returns;
- * from pinned (page-locked) memory the copy runs on the server's upload
- * stream, so `lights` must stay unchanged until the first request that uses
- * the set has completed (cf_server_update_light_set likewise). */
+ * rule: from pageable memory `lights` is copied before the call returns and
+ * is then free to reuse; from pinned (page-locked, 16-byte aligned) memory
+ * the call makes no copy: the server's worker reads `lights` from the device,
+ * together with the other queued uploads and jitters, before the next batch
+ * (or within a few ms when idle), so `lights` must stay allocated and
+ * unchanged until the first request that uses the set has completed, and at
+ * least until cf_server_destroy if none does (cf_server_update_light_set
+ * likewise). */
 CFCULL_API int cf_server_register_light_set(CfServer* server, const CfLightData* lights, uint32_t count, uint64_t* id);
 /* Replaces a set's lights for requests submitted from now on (copy on write:
  * a request binds the set's version current when it is submitted). */

@@ -178,3 +178,44 @@ def test_queued_jitters_chains_releases_and_idle_flush(gpu, oracle):
         assert np.array_equal(cells, oc) and np.array_equal(idx, oi), rid
         srv.release(rid)
     srv.close()
+
+
+def test_pinned_registers_and_updates_are_copied_by_the_worker(gpu, oracle):
+    """From pinned memory a register or an update queues its copy: the worker
+    reads the host buffers from the device (up to 48 per launch) ahead of the
+    queued jitters and the next batch.  60 pinned sets at once, a jitter of a
+    set whose copy is still queued, an update followed by a jitter, and a
+    pinned buffer that is not 16-byte aligned (copied at once instead)."""
+    torch = pytest.importorskip("torch")
+    from hellovulkan_gb300.server import Server
+    from oracle import jitter_lights
+    srv = Server(gpu, budget_bytes=1 << 30, max_batch_views=8, streams=2)
+    rng = np.random.default_rng(6)
+    v = scenes.plain_small(5)
+    sets = [np.ascontiguousarray(scenes.uniform_box_lights(rng, int(n), [-20, -10, -60], [20, 10, -1], 1.0, 6.0),
+                                 np.float32) for n in rng.integers(1, 3000, 60)]
+    pinned = [torch.from_numpy(s).pin_memory() for s in sets]
+    ids = [srv.register(p.numpy()) for p in pinned]
+    expect = {srv.submit(v.ubo, sid): s for sid, s in zip(ids, sets)}
+    a = srv.register(pinned[0].numpy())
+    srv.jitter(a, 3, 0.5)  # reads the version the queued copy writes
+    expect[srv.submit(v.ubo, a)] = jitter_lights(sets[0], 3, 0.5)
+    srv.update(ids[1], pinned[2].numpy())
+    expect[srv.submit(v.ubo, ids[1])] = sets[2]
+    srv.jitter(ids[1], 4, 0.5)
+    expect[srv.submit(v.ubo, ids[1])] = jitter_lights(sets[2], 4, 0.5)
+    flat = torch.empty(sets[3].size + 1, dtype=torch.float32).pin_memory()
+    flat[1:] = torch.from_numpy(sets[3].reshape(-1))
+    odd = flat[1:].numpy().reshape(-1, 12)  # 4 bytes past a 16-byte boundary
+    assert odd.ctypes.data % 16 == 4
+    b = srv.register(odd)
+    expect[srv.submit(v.ubo, b)] = sets[3]
+    done = take(srv, len(expect))
+    for rid, lights in expect.items():
+        assert done[rid].status == 0
+        cells, idx = srv.read(done[rid])
+        oc, oi = oracle_result(oracle, v.ubo, lights)
+        assert np.array_equal(cells, oc) and np.array_equal(idx, oi), rid
+        srv.release(rid)
+    srv.close()
+    del pinned, flat

@@ -521,8 +521,11 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
     bool done = true;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-        w.cnt[k] = 0;
         const uint32_t c = cl0 + k;
+        // A cluster past the view starts full, so nothing is ever written for
+        // it: its +inf box still reaches a light with a NaN coordinate (the
+        // squared distance counts a NaN axis as 0).
+        w.cnt[k] = c < cl_end ? 0u : v.cap;
         if (c < cl_end) {
             const float4 a = v.aabbs[2 * (size_t)c];
             const float4 b = v.aabbs[2 * (size_t)c + 1];
@@ -814,7 +817,10 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
         }
 #pragma unroll
         for (int k = 0; k < K; ++k) {
-            w.cnt[k] = 0;
+            // a cluster past the item (the slice's short last group) starts
+            // full, so nothing is written for it: its +inf box below still
+            // reaches a light with a NaN coordinate
+            w.cnt[k] = cl0 + k < d.cl_end ? 0u : d.cap;
             if (cl0 + k < d.cl_end) {
                 const float4 lo = gb[2 * k], hi = gb[2 * k + 1];
                 const float mn[3] = {lo.x, lo.y, lo.z}, mx[3] = {hi.x, hi.y, hi.z};
@@ -831,7 +837,7 @@ __global__ void __launch_bounds__((WARPS + 1) * 32, WARPS == 4 ? 5 : 3)
         if (lane == 0) {
 #pragma unroll
             for (int k = 0; k < K; ++k)
-                if (cl0 + k >= d.cl_end) {  // past the item: a box that never hits
+                if (cl0 + k >= d.cl_end) {  // past the item: a box no finite light reaches
                     gb[2 * k] = make_float4(inf, inf, inf, 0.f);
                     gb[2 * k + 1] = make_float4(inf, inf, inf, 0.f);
                 }

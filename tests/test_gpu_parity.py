@@ -72,6 +72,24 @@ def test_dense_slices_with_a_short_last_group(gpu, oracle, tuning):
     assert_matches_oracle(oracle, v, *run_pipeline(gpu, v, tuning))
 
 
+@pytest.mark.parametrize("tuning", TUNINGS + [None])
+def test_nan_lights_where_a_warp_holds_a_cluster_past_the_end(gpu, oracle, tuning):
+    """A warp's cluster past the end of its item (a slice's short last group,
+    or the view's last group for the brute-force kernel) holds a +inf box,
+    which a light with a NaN coordinate still reaches: the shader's test
+    counts a NaN axis as 0.  15x9 clusters per slice and 945 in all put such a
+    cluster in the same warp as real ones for every K > 1; nothing may be
+    written for it (it would land in the next slice's lists, or past the
+    staging rows)."""
+    rng = np.random.default_rng(29)
+    lights = scenes.uniform_box_lights(rng, 600, [-20, -10, -60], [20, 10, -1], 1.0, 6.0)
+    lights[[3, 100, 301, 450], 0] = np.nan
+    lights[7, 1] = np.nan
+    lights[222, 2] = np.nan
+    v = scenes.custom_view((15, 9, 7), 1920, 1080, 0.1, 300.0, lights=lights)
+    assert_matches_oracle(oracle, v, *run_pipeline(gpu, v, tuning))
+
+
 @pytest.mark.parametrize("n_lights", [1, 31, 33, 64, 65, 4097, 8193])
 def test_list_segments_around_the_split(gpu, oracle, n_lights):
     """A binned single view bins each slice with two CTAs, one per half of

@@ -126,7 +126,7 @@ class CfServerStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("submitted", "completed", "batches", "views_launched", "max_pending",
                                           "evictions", "arena_bytes", "arena_used_bytes", "arena_peak_bytes",
                                           "pending", "resident_light_sets", "resident_projections")] + [
-        ("max_batch_views", C.c_uint32), ("_pad", C.c_uint32)]
+        ("max_batch_views", C.c_uint32), ("max_held_outputs", C.c_uint32)]
 
 
 class CfServeLoad(C.Structure):
@@ -252,6 +252,7 @@ _SIGS = {
     "cf_server_submit": [_P, C.POINTER(CfServerRequest), _PU64],
     "cf_server_poll": [_P, C.POINTER(CfServerCompletion), _U32, _PU32, _I],
     "cf_server_release": [_P, _U64],
+    "cf_server_release_many": [_P, C.c_void_p, C.c_uint32],
     "cf_server_set_tuning": [_P, _U32, _I, _I, _I, _I],
     "cf_server_get_stats": [_P, C.POINTER(CfServerStats)],
     "cf_serve_run_load": [_P, C.POINTER(CfServeLoad), C.POINTER(CfServeReport)],

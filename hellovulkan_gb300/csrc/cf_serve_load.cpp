@@ -7,8 +7,9 @@
 // after moving every light by a jitter of the given sigma on the device
 // (cf_server_jitter_light_set), otherwise it registers a new set copied from
 // a pool of pre-generated light sets.  Sets that leave a thread's window of
-// recent sets are released.  A poller thread releases each completion's
-// outputs and records its latency from the scheduled arrival.  All random
+// recent sets are released.  A poller thread records each completion's
+// latency from the scheduled arrival and releases the outputs of each poll
+// in one cf_server_release_many call.  All random
 // draws come from std::mt19937_64 seeded by `seed`.
 #include <algorithm>
 #include <atomic>
@@ -151,6 +152,8 @@ extern "C" int cf_serve_run_load(CfServer* server, const CfServeLoad* load, CfSe
     };
 
     std::vector<CfServerCompletion> buf(4096);
+    std::vector<uint64_t> done_ids;
+    done_ids.reserve(buf.size());
     std::atomic<size_t> completed{0}, failed{0};
     double last_done = 0.0;
     auto poller = [&]() {
@@ -158,11 +161,12 @@ extern "C" int cf_serve_run_load(CfServer* server, const CfServeLoad* load, CfSe
             uint32_t got = 0;
             cf_server_poll(server, buf.data(), (uint32_t)buf.size(), &got, 1);
             const double now = secs(clk::now());
+            done_ids.clear();
             for (uint32_t k = 0; k < got; ++k) {
                 const CfServerCompletion& c = buf[k];
                 const size_t i = (size_t)c.user_tag;
                 if (c.status == CF_SUCCESS) {
-                    cf_server_release(server, c.request_id);
+                    done_ids.push_back(c.request_id);
                     latency[i] = submit_lag[i] + (c.t_complete - c.t_submit);
                     queue[i] = submit_lag[i] + (c.t_launch - c.t_submit);
                     exec[i] = c.t_complete - c.t_launch;
@@ -173,6 +177,8 @@ extern "C" int cf_serve_run_load(CfServer* server, const CfServeLoad* load, CfSe
                 }
                 last_done = now;
             }
+            // every output of this poll back to the server under one lock
+            if (!done_ids.empty()) cf_server_release_many(server, done_ids.data(), (uint32_t)done_ids.size());
             if (submitting_done && completed + failed >= submitted) break;
         }
     };

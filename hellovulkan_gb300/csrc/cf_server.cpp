@@ -200,6 +200,7 @@ struct CfServer {
     std::map<uint32_t, cfk::CullConfig> tuned;
     std::thread worker;
     bool stop = false;
+    bool waiting_for_memory = false;  // the worker sleeps until memory returns to the arena
     cudaStream_t upload = nullptr;
     uint64_t next_set = 1, next_req = 1, tick = 0;
     uint64_t memory_epoch = 0;  // bumped whenever device memory returns to the arena
@@ -298,6 +299,7 @@ void complete_request(CfServer* s, Request* r, int status)
         c.d_indices = idx;
         c.d_total = total;
         s->holding[r->id] = r;
+        s->stats.max_held_outputs = std::max<uint32_t>(s->stats.max_held_outputs, (uint32_t)s->holding.size());
     } else {
         s->arena.release(r->out);
         delete r;
@@ -681,13 +683,16 @@ void worker_main(CfServer* s)
         }
         const bool busy = std::any_of(s->slots.begin(), s->slots.end(), [](const StreamSlot& x) { return x.busy; });
         if (s->stop && s->pending.empty() && !busy && s->finished_n.load() == 0) break;
-        if (!launched)
+        if (!launched) {
+            s->waiting_for_memory = blocked_at != UINT64_MAX;  // only then does a release wake the worker
             s->cv.wait_for(lk, std::chrono::milliseconds(2), [s, blocked_at] {
                 if (s->stop || s->finished_n.load() > 0) return true;
                 if (blocked_at != UINT64_MAX) return s->memory_epoch != blocked_at;  // wait for freed memory
                 return !s->pending.empty() &&
                        std::any_of(s->slots.begin(), s->slots.end(), [](const StreamSlot& x) { return !x.busy; });
             });
+            s->waiting_for_memory = false;
+        }
     }
 }
 
@@ -952,7 +957,7 @@ int cf_server_release_light_set(CfServer* s, uint64_t id)
     free_version_if_dead(s, it->second.cur);
     s->sets.erase(it);
     s->memory_epoch++;
-    s->cv.notify_all();
+    if (s->waiting_for_memory) s->cv.notify_all();
     return CF_SUCCESS;
 }
 
@@ -1016,16 +1021,32 @@ int cf_server_poll(CfServer* s, CfServerCompletion* out, uint32_t max, uint32_t*
 
 int cf_server_release(CfServer* s, uint64_t request_id)
 {
-    if (!s) return fail(CF_ERROR_INVALID_ARGUMENT, "null server");
+    return cf_server_release_many(s, &request_id, 1);
+}
+
+int cf_server_release_many(CfServer* s, const uint64_t* request_ids, uint32_t n)
+{
+    if (!s || (n && !request_ids)) return fail(CF_ERROR_INVALID_ARGUMENT, "null argument");
     std::lock_guard<std::mutex> lk(s->mu);
-    auto it = s->holding.find(request_id);
-    if (it == s->holding.end()) return fail(CF_ERROR_INVALID_ARGUMENT, "request %llu holds no outputs",
-                                            (unsigned long long)request_id);
-    s->arena.release(it->second->out);
-    delete it->second;
-    s->holding.erase(it);
-    s->memory_epoch++;
-    s->cv.notify_all();
+    uint64_t unknown = 0;
+    uint32_t n_unknown = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        auto it = s->holding.find(request_ids[i]);
+        if (it == s->holding.end()) {
+            if (!n_unknown++) unknown = request_ids[i];
+            continue;
+        }
+        s->arena.release(it->second->out);
+        delete it->second;
+        s->holding.erase(it);
+    }
+    if (n_unknown < n) {
+        s->memory_epoch++;
+        if (s->waiting_for_memory) s->cv.notify_all();
+    }
+    if (n_unknown)
+        return fail(CF_ERROR_INVALID_ARGUMENT, "%u request(s) hold no outputs, the first %llu", n_unknown,
+                    (unsigned long long)unknown);
     return CF_SUCCESS;
 }
 

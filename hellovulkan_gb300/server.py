@@ -81,6 +81,11 @@ class Server:
     def release(self, request_id: int) -> None:
         check(lib().cf_server_release(self.handle, request_id))
 
+    def release_many(self, request_ids) -> None:
+        """release() for many requests under one acquisition of the server's lock."""
+        ids = (C.c_uint64 * len(request_ids))(*request_ids)
+        check(lib().cf_server_release_many(self.handle, C.cast(ids, C.c_void_p), len(request_ids)))
+
     def read(self, c: CfServerCompletion, cap: int = 150):
         """(cells (C,2) uint32, indices (total,) uint32) of a successful completion."""
         from .pipelines import device_view

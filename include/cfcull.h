@@ -305,7 +305,7 @@ typedef struct CfServerCompletion {
 typedef struct CfServerStats {
     uint64_t submitted, completed, batches, views_launched, max_pending, evictions;
     uint64_t arena_bytes, arena_used_bytes, arena_peak_bytes, pending, resident_light_sets, resident_projections;
-    uint32_t max_batch_views, _pad;
+    uint32_t max_batch_views, max_held_outputs; /* most completed requests at once whose outputs were not released */
 } CfServerStats;
 
 CFCULL_API int cf_server_create(CfContext* ctx, const CfServerConfig* config, CfServer** out);
@@ -345,6 +345,11 @@ CFCULL_API int cf_server_submit(CfServer* server, const CfServerRequest* request
 CFCULL_API int cf_server_poll(CfServer* server, CfServerCompletion* out, uint32_t max, uint32_t* count, int wait_ms);
 /* Returns a completed request's device results to the budget. */
 CFCULL_API int cf_server_release(CfServer* server, uint64_t request_id);
+/* cf_server_release for n requests under one acquisition of the server's
+ * lock (a poller releasing what one cf_server_poll returned).  Ids that hold
+ * no outputs are skipped; the call then returns CF_ERROR_INVALID_ARGUMENT
+ * after releasing every other one. */
+CFCULL_API int cf_server_release_many(CfServer* server, const uint64_t* request_ids, uint32_t n);
 CFCULL_API int cf_server_set_tuning(CfServer* server, uint32_t slice_clusters, int clusters_per_warp, int warps,
                                     int tile, int stages);
 CFCULL_API int cf_server_get_stats(CfServer* server, CfServerStats* stats);

@@ -172,6 +172,7 @@ static void abi_argument_checks()
     CHECK(cf_cull_workspace_size(&bad, 10, 150, &ws) == CF_ERROR_INVALID_ARGUMENT);  // too many clusters
     CHECK(cf_cull_lights(nullptr, nullptr, nullptr, 0, 150, nullptr, nullptr, 0, nullptr, nullptr, 0, nullptr) ==
           CF_ERROR_INVALID_ARGUMENT);
+    CHECK(cf_server_release_many(nullptr, nullptr, 0) == CF_ERROR_INVALID_ARGUMENT);
     CHECK(cf_testing_inject_stall(0x80u) == CF_ERROR_INVALID_ARGUMENT);
     CHECK(cf_testing_fail_allocation_after(-1) == CF_SUCCESS);
     CHECK(std::strlen(cf_last_error_message()) > 0);

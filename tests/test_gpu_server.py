@@ -102,6 +102,26 @@ def test_copy_on_write_updates_and_device_jitter(gpu, oracle):
     srv.close()
 
 
+def test_release_many_returns_every_output_and_reports_unknown_ids(gpu):
+    from hellovulkan_gb300 import CfError
+    from hellovulkan_gb300.server import Server
+    srv = Server(gpu, budget_bytes=256 << 20)
+    v = scenes.plain_small(6)
+    sid = srv.register(v.lights)
+    ids = [srv.submit(v.ubo, sid) for _ in range(12)]
+    take(srv, len(ids))
+    held = srv.stats()["arena_used_bytes"]
+    with pytest.raises(CfError) as e:
+        srv.release_many(ids + [10 ** 9])  # one id that holds nothing: the others are still released
+    assert e.value.status == 1  # CF_ERROR_INVALID_ARGUMENT
+    assert srv.stats()["arena_used_bytes"] < held
+    with pytest.raises(CfError):
+        srv.release(ids[0])  # already released
+    srv.release_many([])
+    assert srv.stats()["max_held_outputs"] == 12
+    srv.close()
+
+
 def test_budget_admission_and_eviction(gpu):
     from hellovulkan_gb300 import CfError
     from hellovulkan_gb300.server import Server

@@ -483,7 +483,7 @@ def measured_once_more_after_stall(run_fn):
 
 def measure_serve(ctx, seconds, rates=(2000.0, 10000.0, 50000.0), sweep=(20000.0, 40000.0, 60000.0, 80000.0,
                                                                         90000.0, 100000.0, 110000.0, 120000.0,
-                                                                        150000.0, 200000.0),
+                                                                        130000.0, 140000.0, 150000.0, 200000.0),
                   sweep_seconds=5.0, submit_threads=4):
     """The served stream: Poisson arrivals at each rate for `seconds`, requests
     drawn like the batched mix (4 projections, random cameras, 128 base light

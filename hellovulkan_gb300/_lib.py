@@ -253,6 +253,7 @@ _SIGS = {
     "cf_server_poll": [_P, C.POINTER(CfServerCompletion), _U32, _PU32, _I],
     "cf_server_release": [_P, _U64],
     "cf_server_release_many": [_P, C.c_void_p, C.c_uint32],
+    "cf_server_declare_pinned_host": [_P, C.c_void_p, C.c_size_t],
     "cf_server_set_tuning": [_P, _U32, _I, _I, _I, _I],
     "cf_server_get_stats": [_P, C.POINTER(CfServerStats)],
     "cf_serve_run_load": [_P, C.POINTER(CfServeLoad), C.POINTER(CfServeReport)],

@@ -6,11 +6,11 @@
 // p_reuse it re-references one of the submitting thread's recent light sets
 // after moving every light by a jitter of the given sigma on the device
 // (cf_server_jitter_light_set), otherwise it registers a new set copied from
-// a pool of pre-generated light sets.  Sets that leave a thread's window of
-// recent sets are released.  A poller thread records each completion's
-// latency from the scheduled arrival and releases the outputs of each poll
-// in one cf_server_release_many call.  All random
-// draws come from std::mt19937_64 seeded by `seed`.
+// a pool of pre-generated light sets (declared to the server when pinned).
+// Sets that leave a thread's window of recent sets are released.  A poller
+// thread records each completion's latency from the scheduled arrival and
+// releases the outputs of each poll in one cf_server_release_many call.  All
+// random draws come from std::mt19937_64 seeded by `seed`.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -73,6 +73,12 @@ extern "C" int cf_serve_run_load(CfServer* server, const CfServeLoad* load, CfSe
     if (!server || !load || !report || !load->projections || !load->n_projections || !load->n_base_sets ||
         !load->base_sets || !load->base_counts || load->rate_per_s <= 0 || load->duration_s <= 0)
         return fail(CF_ERROR_INVALID_ARGUMENT, "cf_serve_run_load: bad argument");
+    // a client with a pinned pool declares it once, so that its registers make
+    // no CUDA call (pageable sets fail the declaration and are copied per call)
+    for (uint32_t b = 0; b < load->n_base_sets; ++b)
+        if (load->base_sets[b] && load->base_counts[b])
+            (void)cf_server_declare_pinned_host(server, load->base_sets[b],
+                                                (size_t)load->base_counts[b] * sizeof(CfLightData));
     const uint32_t threads = std::max(1u, load->submit_threads);
     const uint32_t window = std::max(1u, load->recent_sets / threads);
     // arrival schedule

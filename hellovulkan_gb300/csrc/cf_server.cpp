@@ -30,8 +30,11 @@
 #include <memory>
 #include <mutex>
 #include <new>
+#include <shared_mutex>
 #include <thread>
 #include <vector>
+
+#include <unistd.h>
 
 #include "cf_arena.h"
 #include "cf_batch_internal.h"
@@ -75,6 +78,13 @@ struct VersionJob {
     const void* host;
     uint64_t seed;
     float sigma;
+};
+
+// A host range the client declared pinned for the server's lifetime
+// (cf_server_declare_pinned_host): [begin, end) on the host, read by the
+// device at dev + (address - begin).
+struct PinnedRange {
+    uintptr_t begin, end, dev;
 };
 
 struct LightSet {
@@ -186,6 +196,10 @@ struct CfServer {
     std::condition_variable cv, done_cv;
     std::deque<Request*> pending;
     std::vector<VersionJob> jobs;  // queued uploads and jitters, launched before the next batch
+    // declared pinned host ranges, sorted and disjoint; read on every register
+    // and update, written only by declarations, so behind their own lock
+    std::shared_mutex pinned_mu;
+    std::vector<PinnedRange> pinned;
     std::vector<StreamSlot> slots;
     std::map<uint64_t, LightSet> sets;
     std::vector<AabbEntry*> aabbs;
@@ -305,8 +319,7 @@ void complete_request(CfServer* s, Request* r, int status)
         delete r;
     }
     s->completions.push_back(c);
-    s->stats.completed++;
-    s->done_cv.notify_all();
+    s->stats.completed++;  // pollers are woken once per worker pass (worker_main)
 }
 
 // Takes what request r needs; false (nothing taken) when the arena is full.
@@ -388,14 +401,12 @@ void take_finished(CfServer* s, std::deque<Batch*>& out)
     s->finished_n.fetch_sub((uint32_t)out.size());
 }
 
-// Writes the batch's tables into the slot's pinned block and decides which
-// AABBs it generates or waits for (server lock held).
-void plan_batch(CfServer* s, int slot_i, const std::vector<Request*>& reqs, LaunchPlan& plan)
+// Decides which AABB entries the batch generates and which it waits for
+// (`mu` held: the entries' flags are shared with other batches).
+void plan_batch(const std::vector<Request*>& reqs, LaunchPlan& plan)
 {
-    StreamSlot& sl = s->slots[slot_i];
-    const uint32_t n = (uint32_t)reqs.size();
     plan = LaunchPlan{};
-    plan.views = n;
+    plan.views = (uint32_t)reqs.size();
     for (Request* r : reqs) {
         AabbEntry* a = r->aabb;
         if (!a->generated) {
@@ -406,6 +417,17 @@ void plan_batch(CfServer* s, int slot_i, const std::vector<Request*>& reqs, Laun
             plan.wait.push_back(a);
         }
     }
+}
+
+// Writes the batch's tables into its slot's pinned block and plans its
+// launches.  Called WITHOUT `mu`: the slot and the admitted requests (their
+// memory, versions and AABB entries, all held by reference) are the worker's
+// until the batch's host callback runs, and submitters should not wait while
+// thousands of work items are written.
+void fill_tables(CfServer* s, int slot_i, const std::vector<Request*>& reqs, LaunchPlan& plan)
+{
+    StreamSlot& sl = s->slots[slot_i];
+    const uint32_t n = plan.views;
     // items are counted first: their section follows the jobs and prefixes
     uint32_t items = 0;
     for (Request* r : reqs) items += r->groups;
@@ -587,6 +609,7 @@ void worker_main(CfServer* s)
     std::unique_lock<std::mutex> lk(s->mu);
     uint64_t blocked_at = UINT64_MAX;  // memory epoch at which the head request did not fit
     for (;;) {
+        const uint64_t completed_before = s->stats.completed;
         std::deque<Batch*> done;
         take_finished(s, done);
         for (Batch* b : done) finish_batch(s, b);
@@ -630,7 +653,7 @@ void worker_main(CfServer* s)
                 break;
             }
             LaunchPlan plan;
-            plan_batch(s, (int)q, batch, plan);
+            plan_batch(batch, plan);
             s->slots[q].busy = true;
             const double t_launch = now_s();
             for (Request* r : batch) r->t_launch = t_launch;
@@ -641,6 +664,7 @@ void worker_main(CfServer* s)
             std::vector<VersionJob> jobs;
             jobs.swap(s->jobs);
             lk.unlock();
+            fill_tables(s, (int)q, batch, plan);
             int st = launch_jobs(s, jobs);
             if (st == CF_SUCCESS) st = enqueue_batch(s, (int)q, plan, batch);
             lk.lock();
@@ -681,6 +705,7 @@ void worker_main(CfServer* s)
                 s->jobs.swap(jobs);
             }
         }
+        if (s->stats.completed != completed_before) s->done_cv.notify_all();  // one wake-up per pass, not per request
         const bool busy = std::any_of(s->slots.begin(), s->slots.end(), [](const StreamSlot& x) { return x.busy; });
         if (s->stop && s->pending.empty() && !busy && s->finished_n.load() == 0) break;
         if (!launched) {
@@ -725,6 +750,31 @@ const void* device_view_of_pinned(CfServer* s, const void* host)
     if (a.type != cudaMemoryTypeHost || !a.devicePointer || (reinterpret_cast<uintptr_t>(a.devicePointer) & 15u))
         return nullptr;
     return a.devicePointer;
+}
+
+// The device-side address of `host` .. `host` + bytes when the range lies
+// inside one declared pinned range (and is 16-byte aligned there), else null.
+// No CUDA call.
+const void* declared_view(CfServer* s, const void* host, size_t bytes)
+{
+    const uintptr_t b = reinterpret_cast<uintptr_t>(host);
+    std::shared_lock<std::shared_mutex> lk(s->pinned_mu);
+    auto it = std::upper_bound(s->pinned.begin(), s->pinned.end(), b,
+                               [](uintptr_t x, const PinnedRange& r) { return x < r.begin; });
+    if (it == s->pinned.begin()) return nullptr;
+    const PinnedRange& r = *std::prev(it);
+    if (b < r.begin || bytes > r.end - b) return nullptr;
+    const uintptr_t d = r.dev + (b - r.begin);
+    return (d & 15u) ? nullptr : reinterpret_cast<const void*>(d);
+}
+
+// Where the device reads `count` lights at `host` from: a declared range, else
+// whatever the CUDA runtime reports (null: pageable, copied at once).
+const void* device_view_of(CfServer* s, const CfLightData* host, uint32_t count)
+{
+    if (!count) return nullptr;
+    const void* d = declared_view(s, host, (size_t)count * sizeof(CfLightData));
+    return d ? d : device_view_of_pinned(s, host);
 }
 
 // Enqueues the copy that fills v on the upload stream.  Called WITHOUT `mu`:
@@ -836,11 +886,50 @@ int cf_server_destroy(CfServer* s)
     return CF_SUCCESS;
 }
 
+int cf_server_declare_pinned_host(CfServer* s, const void* host, size_t bytes)
+{
+    if (!s || !host || !bytes) return fail(CF_ERROR_INVALID_ARGUMENT, "null or empty range");
+    const uintptr_t b = reinterpret_cast<uintptr_t>(host), e = b + bytes;
+    if (e < b) return fail(CF_ERROR_INVALID_ARGUMENT, "range wraps around");
+    long page = sysconf(_SC_PAGESIZE);
+    if (page <= 0) page = 4096;
+    // the first byte, every page start inside, the last byte: each pinned and
+    // mapped at the same offset from the first, so the device may read any of it
+    DeviceGuard g(s->device);
+    uintptr_t dev0 = 0;
+    for (uintptr_t p = b;;) {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, reinterpret_cast<const void*>(p)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(CF_ERROR_INVALID_ARGUMENT, "host range is not known to CUDA");
+        }
+        if (a.type != cudaMemoryTypeHost || !a.devicePointer)
+            return fail(CF_ERROR_INVALID_ARGUMENT, "host range is not pinned and mapped for the device");
+        const uintptr_t d = reinterpret_cast<uintptr_t>(a.devicePointer);
+        if (p == b) dev0 = d;
+        else if (d - dev0 != p - b) return fail(CF_ERROR_INVALID_ARGUMENT, "host range is not one linear mapping");
+        if (p == e - 1) break;
+        const uintptr_t next = (p / (uintptr_t)page + 1) * (uintptr_t)page;
+        p = next < e - 1 ? next : e - 1;
+    }
+    std::unique_lock<std::shared_mutex> lk(s->pinned_mu);
+    auto it = std::upper_bound(s->pinned.begin(), s->pinned.end(), b,
+                               [](uintptr_t x, const PinnedRange& r) { return x < r.begin; });
+    if (it != s->pinned.begin()) {
+        const PinnedRange& q = *std::prev(it);
+        if (q.begin == b && q.end == e) return CF_SUCCESS;  // declared before
+        if (q.end > b) return fail(CF_ERROR_INVALID_ARGUMENT, "overlaps a declared range");
+    }
+    if (it != s->pinned.end() && it->begin < e) return fail(CF_ERROR_INVALID_ARGUMENT, "overlaps a declared range");
+    s->pinned.insert(it, PinnedRange{b, e, dev0});
+    return CF_SUCCESS;
+}
+
 int cf_server_register_light_set(CfServer* s, const CfLightData* lights, uint32_t count, uint64_t* id)
 {
     if (!s || !id || (count && !lights)) return fail(CF_ERROR_INVALID_ARGUMENT, "null argument");
     if (count > kMaxLights) return fail(CF_ERROR_INVALID_ARGUMENT, "too many lights");
-    const void* mapped = count ? device_view_of_pinned(s, lights) : nullptr;
+    const void* mapped = device_view_of(s, lights, count);
     LightVersion* v = nullptr;
     {
         std::lock_guard<std::mutex> lk(s->mu);
@@ -891,7 +980,7 @@ int publish_version(CfServer* s, uint64_t id, LightVersion* v, LightVersion* pin
 int cf_server_update_light_set(CfServer* s, uint64_t id, const CfLightData* lights, uint32_t count)
 {
     if (!s || (count && !lights)) return fail(CF_ERROR_INVALID_ARGUMENT, "null argument");
-    const void* mapped = count ? device_view_of_pinned(s, lights) : nullptr;
+    const void* mapped = device_view_of(s, lights, count);
     LightVersion *v = nullptr, *old = nullptr;
     {
         std::lock_guard<std::mutex> lk(s->mu);

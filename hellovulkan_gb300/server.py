@@ -81,6 +81,14 @@ class Server:
     def release(self, request_id: int) -> None:
         check(lib().cf_server_release(self.handle, request_id))
 
+    def declare_pinned(self, arr) -> None:
+        """Declares a pinned host array (a pinned tensor or its numpy view) for
+        the server's lifetime: registers and updates from it make no CUDA
+        call.  The server object keeps a reference to it."""
+        a = arr.numpy() if hasattr(arr, "numpy") else arr
+        check(lib().cf_server_declare_pinned_host(self.handle, a.ctypes.data, a.nbytes))
+        self._keep_alive = getattr(self, "_keep_alive", []) + [arr]
+
     def release_many(self, request_ids) -> None:
         """release() for many requests under one acquisition of the server's lock."""
         ids = (C.c_uint64 * len(request_ids))(*request_ids)

@@ -324,6 +324,15 @@ CFCULL_API int cf_server_destroy(CfServer* server);
  * least until cf_server_destroy if none does (cf_server_update_light_set
  * likewise). */
 CFCULL_API int cf_server_register_light_set(CfServer* server, const CfLightData* lights, uint32_t count, uint64_t* id);
+/* Declares host memory [host, host + bytes) pinned for the server's lifetime:
+ * the caller keeps it allocated and page-locked until cf_server_destroy.
+ * Registers and updates whose lights lie inside a declared range then make no
+ * CUDA call at all (an undeclared pointer costs one cudaPointerGetAttributes).
+ * Every page is checked once here: CF_ERROR_INVALID_ARGUMENT if any is not
+ * pinned and mapped for the device, the mapping is not linear, or the range
+ * overlaps another declared range (declaring the same range again is a
+ * no-op).  A client with a pool of pinned staging buffers declares the pool. */
+CFCULL_API int cf_server_declare_pinned_host(CfServer* server, const void* host, size_t bytes);
 /* Replaces a set's lights for requests submitted from now on (copy on write:
  * a request binds the set's version current when it is submitted). */
 CFCULL_API int cf_server_update_light_set(CfServer* server, uint64_t id, const CfLightData* lights, uint32_t count);
@@ -361,7 +370,10 @@ CFCULL_API int cf_server_get_stats(CfServer* server, CfServerStats* stats);
  * [target_lo, target_hi]) and, with probability p_reuse, one of its
  * submitting thread's recent light sets moved by cf_server_jitter_light_set
  * (sigma jitter_sigma), else a new set copied from base_sets.  recent_sets
- * is split across submit_threads; sets leaving a window are released. */
+ * is split across submit_threads; sets leaving a window are released.  Base
+ * sets in pinned memory are declared to the server first
+ * (cf_server_declare_pinned_host), so they must stay allocated until
+ * cf_server_destroy; pageable ones are copied at each register. */
 typedef struct CfServeLoad {
     double rate_per_s, duration_s, p_reuse;
     uint64_t seed;

@@ -122,6 +122,45 @@ def test_release_many_returns_every_output_and_reports_unknown_ids(gpu):
     srv.close()
 
 
+def test_declared_pinned_ranges(gpu, oracle):
+    """Registers and updates from inside a declared pinned range make no CUDA
+    call and give the oracle's result; undeclared pinned memory still works;
+    pageable and overlapping declarations are refused."""
+    torch = pytest.importorskip("torch")
+    from hellovulkan_gb300 import CfError
+    from hellovulkan_gb300.server import Server
+    srv = Server(gpu, budget_bytes=256 << 20)
+    rng = np.random.default_rng(8)
+    v = scenes.plain_small(7)
+    pool = torch.from_numpy(np.ascontiguousarray(
+        scenes.uniform_box_lights(rng, 3000, [-20, -10, -60], [20, 10, -1], 1.0, 6.0), np.float32)).pin_memory()
+    srv.declare_pinned(pool)
+    srv.declare_pinned(pool)  # the same range again: a no-op
+    with pytest.raises(CfError) as e:
+        srv.declare_pinned(pool[1000:2000])  # inside a declared range
+    assert e.value.status == 1
+    with pytest.raises(CfError) as e:
+        srv.declare_pinned(np.zeros((100, 12), np.float32))  # pageable
+    assert e.value.status == 1
+    a = pool.numpy()
+    expect = {}
+    s1 = srv.register(a[100:1100])  # 100 lights in: still 16-byte aligned
+    expect[srv.submit(v.ubo, s1)] = a[100:1100].copy()
+    srv.update(s1, a[2000:2900])
+    expect[srv.submit(v.ubo, s1)] = a[2000:2900].copy()
+    other = torch.from_numpy(np.ascontiguousarray(a[:700])).pin_memory()  # pinned, undeclared
+    s2 = srv.register(other.numpy())
+    expect[srv.submit(v.ubo, s2)] = a[:700].copy()
+    done = take(srv, len(expect))
+    for rid, lights in expect.items():
+        cells, idx = srv.read(done[rid])
+        oc, oi = oracle_result(oracle, v.ubo, lights)
+        assert np.array_equal(cells, oc) and np.array_equal(idx, oi), rid
+    srv.release_many(list(expect))
+    srv.close()
+    del other
+
+
 def test_budget_admission_and_eviction(gpu):
     from hellovulkan_gb300 import CfError
     from hellovulkan_gb300.server import Server

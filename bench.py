@@ -481,16 +481,16 @@ def measured_once_more_after_stall(run_fn):
     return x
 
 
-def measure_serve(ctx, seconds, rates=(2000.0, 10000.0, 50000.0), sweep=(20000.0, 40000.0, 60000.0, 80000.0,
-                                                                        90000.0, 100000.0, 110000.0, 120000.0,
-                                                                        130000.0, 140000.0, 150000.0, 200000.0),
-                  sweep_seconds=5.0, submit_threads=4):
+def measure_serve(ctx, seconds, rates=(2000.0, 10000.0, 50000.0), sweep=(60000.0, 80000.0, 90000.0, 100000.0,
+                                                                        110000.0, 120000.0, 130000.0, 140000.0,
+                                                                        150000.0, 200000.0),
+                  sweep_seconds=10.0, submit_threads=4):
     """The served stream: Poisson arrivals at each rate for `seconds`, requests
     drawn like the batched mix (4 projections, random cameras, 128 base light
     sets of 256..65536 blob lights), light sets re-referenced with p = 0.7 and
     jittered on the device by N(0, 0.1) per request, an 8 GiB device budget.
     Latency runs from the scheduled arrival to the completion callback.  A
-    sweep of shorter runs then finds the highest offered rate the server
+    sweep of 10 s runs then finds the highest offered rate the server
     sustains with p99 <= 2 ms (stopping at the first rate that misses)."""
     from hellovulkan_gb300.server import Server, run_load
     keep = ("offered_rate", "achieved_rate", "scheduled", "completed", "failed", "latency_p50_ms", "latency_p90_ms",

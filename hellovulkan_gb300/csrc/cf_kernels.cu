@@ -284,31 +284,20 @@ struct WarpClusters {
     float mn[K][3];
     float mx[K][3];
     uint32_t cnt[K];
-    float umn[3], umx[3];  // union of the warp's valid boxes (NaN bounds widen it to +-inf)
 };
 
-// Tests the lights of one shared-memory tile against the warp's K clusters;
-// returns true once every cluster of the warp has reached the cap.
+// Tests the lights of one shared-memory tile (lights base .. base + n - 1)
+// against the warp's K clusters of the brute-force kernel; returns true once
+// every cluster of the warp has reached the cap.
 //   kExact   the shader's branchy test (tiles holding non-finite coordinates)
-//   kBinned  light indices come from idx_tile (a slice candidate list) instead
-//            of base + position, and each 32-light chunk is first tested
-//            against the warp's union box: a chunk no lane of which can reach
-//            the union cannot hit any of the K boxes (per axis the distance
-//            to a box that contains another is never larger, and the rounded
-//            sums are monotonic), so the K tests are skipped
-template <int K, bool kExact, bool kBinned>
-__device__ __forceinline__ bool scan_tile(const float4* __restrict__ tile, const uint32_t* __restrict__ idx_tile,
-                                          uint32_t n, uint32_t base, uint32_t lane, WarpClusters<K>& w, uint32_t cap,
-                                          uint32_t* __restrict__ staging, uint32_t cl0, uint32_t cl_end,
-                                          uint32_t& chunks_filtered, uint32_t& chunks_tested)
+template <int K, bool kExact>
+__device__ __forceinline__ bool scan_tile(const float4* __restrict__ tile, uint32_t n, uint32_t base, uint32_t lane,
+                                          WarpClusters<K>& w, uint32_t cap, uint32_t* __restrict__ staging,
+                                          uint32_t cl0, uint32_t cl_end, uint32_t& chunks_tested)
 {
     const uint32_t lt_mask = (1u << lane) - 1u;
     for (uint32_t j = 0; j < n; j += 32) {
         const float4 L = tile[j + lane];
-        if (kBinned) {
-            ++chunks_filtered;
-            if (!__any_sync(kFull, hit_fast(L, w.umn, w.umx))) continue;
-        }
         ++chunks_tested;
         bool h[K];
         bool any = false;
@@ -318,7 +307,7 @@ __device__ __forceinline__ bool scan_tile(const float4* __restrict__ tile, const
             any |= h[k];
         }
         if (__any_sync(kFull, any)) {
-            const uint32_t li = kBinned ? idx_tile[j + lane] : base + j + lane;
+            const uint32_t li = base + j + lane;
             bool all_capped = true;
 #pragma unroll
             for (int k = 0; k < K; ++k) {
@@ -538,7 +527,7 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
     }
     if (done && lane == 0) atomicAdd(done_warps, 1u);
 
-    uint32_t chunks_filtered = 0, chunks_tested = 0;
+    uint32_t chunks_tested = 0;
     for (uint32_t t = 0; t < ntiles; ++t) {
         const uint32_t s = t % STAGES;
         if (!mbar_wait_bounded(smem_u32(&full[s]), (t / STAGES) & 1u)) {
@@ -555,11 +544,9 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
             const uint32_t n = min((uint32_t)TILE, nsrc - base);
             const float4* tile = tiles + (size_t)s * TILE;
             if (!tile_has_nonfinite(v.nonfinite, base, n))
-                done = scan_tile<K, false, false>(tile, nullptr, n, base, lane, w, v.cap, v.staging, cl0, cl_end,
-                                                  chunks_filtered, chunks_tested);
+                done = scan_tile<K, false>(tile, n, base, lane, w, v.cap, v.staging, cl0, cl_end, chunks_tested);
             else
-                done = scan_tile<K, true, false>(tile, nullptr, n, base, lane, w, v.cap, v.staging, cl0, cl_end,
-                                                 chunks_filtered, chunks_tested);
+                done = scan_tile<K, true>(tile, n, base, lane, w, v.cap, v.staging, cl0, cl_end, chunks_tested);
             if (done && lane == 0) atomicAdd(done_warps, 1u);
         }
         __syncwarp();
@@ -576,10 +563,7 @@ __global__ void __launch_bounds__((WARPS + 1) * 32) cull_kernel(const ViewCull v
                 sum += w.cnt[k];
             }
         s_gsum[warp] = sum;
-        if (v.work) {
-            atomicAdd(&v.work[0], 32ull * chunks_filtered);
-            atomicAdd(&v.work[1], 32ull * K * chunks_tested);
-        }
+        if (v.work) atomicAdd(&v.work[1], 32ull * K * chunks_tested);  // no filter tests without binning
     }
     consumer_sync<WARPS * 32>();
     if (threadIdx.x == 0) {

@@ -232,6 +232,7 @@ _SIGS = {
     "cf_testing_set_wait_limit_ns": [_U64],
     "cf_testing_inject_stall": [_U32],
     "cf_testing_fail_allocation_after": [C.c_int32],
+    "cf_testing_fail_version_writes": [C.c_int32],
     "cf_batch_create": [_P, C.POINTER(_P)],
     "cf_batch_destroy": [_P],
     "cf_batch_set_views": [_P, C.POINTER(CfBatchView), _U32],

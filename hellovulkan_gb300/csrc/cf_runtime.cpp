@@ -102,7 +102,16 @@ DeviceGuard::~DeviceGuard()
 
 namespace {
 std::atomic<int32_t> g_fail_allocation_after{-1};  // allocations to let through before one fails; < 0: none
+std::atomic<int32_t> g_fail_version_writes{0};     // server version-write launches still to fail
 }  // namespace
+
+bool take_injected_version_write_failure()
+{
+    int32_t n = g_fail_version_writes.load();
+    while (n > 0)
+        if (g_fail_version_writes.compare_exchange_weak(n, n - 1)) return true;
+    return false;
+}
 
 cudaError_t device_malloc(void** ptr, size_t bytes)
 {
@@ -888,6 +897,12 @@ int cf_testing_inject_stall(uint32_t mode)
 int cf_testing_fail_allocation_after(int32_t n)
 {
     set_fail_allocation_after(n);
+    return CF_SUCCESS;
+}
+
+int cf_testing_fail_version_writes(int32_t n)
+{
+    g_fail_version_writes.store(n > 0 ? n : 0);
     return CF_SUCCESS;
 }
 

@@ -49,6 +49,10 @@ private:
 // cudaMalloc, except that a test may make it fail (cf_testing_fail_allocation_after).
 cudaError_t device_malloc(void** ptr, size_t bytes);
 
+// True (and one fewer left) when a test asked the server's next launch of
+// queued light-set uploads and jitters to fail (cf_testing_fail_version_writes).
+bool take_injected_version_write_failure();
+
 // Ensures *ptr holds at least `bytes` of zero-filled device memory.
 int grow(void** ptr, size_t* capacity, size_t bytes, const char* what);
 

@@ -81,6 +81,7 @@ struct LightVersion {
     uint32_t count = 0;
     uint32_t refs = 0;
     bool retired = false;
+    bool failed = false;  // its queued upload or jitter failed to launch: requests bound to it fail
 };
 
 // Work that writes a new version, waiting for the worker: a jitter of `src`,
@@ -344,6 +345,10 @@ bool admit(CfServer* s, Request* r)
 {
     const CfClusterForwardUBO& u = r->req.ubo;
     LightVersion* lv = r->lights;  // bound (and referenced) at submission
+    if (lv->failed) {
+        r->status = CF_ERROR_CUDA;  // its lights were never written
+        return true;
+    }
     const uint32_t xy = u.sliceCountX * u.sliceCountY, Z = u.sliceCountZ;
     r->cfg = server_config_for(s, xy);
     const uint32_t groups = cfk::group_count(r->clusters, xy, Z, (uint32_t)(r->cfg.warps * r->cfg.clusters_per_warp), true);
@@ -592,6 +597,7 @@ void finish_batch(CfServer* s, Batch* b)
 int launch_jobs(CfServer* s, const std::vector<VersionJob>& jobs)
 {
     if (jobs.empty()) return CF_SUCCESS;
+    if (take_injected_version_write_failure()) return fail(CF_ERROR_CUDA, "light set uploads and jitters (injected)");
     std::vector<cfk::UploadTask> uploads;
     std::vector<cfk::JitterTask> jitters;
     for (const VersionJob& j : jobs) {
@@ -605,6 +611,13 @@ int launch_jobs(CfServer* s, const std::vector<VersionJob>& jobs)
     cudaError_t e = cfk::launch_upload_tasks(uploads.data(), (uint32_t)uploads.size(), s->upload);
     if (e == cudaSuccess) e = cfk::launch_jitter_tasks(jitters.data(), (uint32_t)jitters.size(), s->upload);
     return e == cudaSuccess ? CF_SUCCESS : cuda_fail(e, "light set uploads and jitters");
+}
+
+// The versions a failed launch did not write (lock held): every request bound
+// to one fails at admission, and so does a jitter of one.
+void mark_failed(const std::vector<VersionJob>& jobs)
+{
+    for (const VersionJob& j : jobs) j.dst->failed = true;
 }
 
 // Drops the jobs' holds on their versions (lock held).
@@ -682,9 +695,10 @@ void worker_main(CfServer* s)
             jobs.swap(s->jobs);
             lk.unlock();
             fill_tables(s, (int)q, batch, plan);
-            int st = launch_jobs(s, jobs);
-            if (st == CF_SUCCESS) st = enqueue_batch(s, (int)q, plan, batch);
+            const int jst = launch_jobs(s, jobs);
+            const int st = jst == CF_SUCCESS ? enqueue_batch(s, (int)q, plan, batch) : jst;
             lk = take_lock(s->mu);
+            if (jst != CF_SUCCESS) mark_failed(jobs);
             release_jobs(s, jobs);
             if (st != CF_SUCCESS) {
                 s->slots[q].busy = false;
@@ -707,20 +721,15 @@ void worker_main(CfServer* s)
         if (!launched && !s->jobs.empty()) {
             // No batch went out to carry them: launch the queued jobs alone, so
             // that their versions do not hold arena memory (nor their callers'
-            // host buffers) while idle.  If the launch fails they go back to the
-            // queue, and the next batch retries them and reports the failure to
-            // its requests.
+            // host buffers) while idle.  If the launch fails, the versions are
+            // marked failed and their requests report it.
             std::vector<VersionJob> jobs;
             jobs.swap(s->jobs);
             lk.unlock();
             const int st = launch_jobs(s, jobs);
             lk = take_lock(s->mu);
-            if (st == CF_SUCCESS) {
-                release_jobs(s, jobs);
-            } else {
-                jobs.insert(jobs.end(), s->jobs.begin(), s->jobs.end());
-                s->jobs.swap(jobs);
-            }
+            if (st != CF_SUCCESS) mark_failed(jobs);
+            release_jobs(s, jobs);
         }
         if (s->stats.completed != completed_before) s->done_cv.notify_all();  // one wake-up per pass, not per request
         const bool busy = std::any_of(s->slots.begin(), s->slots.end(), [](const StreamSlot& x) { return x.busy; });
@@ -1044,6 +1053,7 @@ int cf_server_jitter_light_set(CfServer* s, uint64_t id, uint64_t seed, float si
     }
     v->d = d;
     v->count = old->count;
+    v->failed = old->failed;  // a jitter of an unwritten version is unwritten too
     // The jitter itself is queued: the worker launches the queued jobs on the
     // upload stream in one go before the next batch's upload fence, so a
     // request that binds the new version reads it only after it is written,

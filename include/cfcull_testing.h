@@ -37,6 +37,11 @@ CFCULL_API int cf_testing_inject_stall(uint32_t mode);
  * one); n < 0 turns this off.  Covers contexts, the pipelines' buffers and
  * workspaces, batches and servers. */
 CFCULL_API int cf_testing_fail_allocation_after(int32_t n);
+/* Makes the servers' next n launches of queued light-set uploads and jitters
+ * fail as a failed launch would (CF_ERROR_CUDA), without launching anything;
+ * n <= 0 turns this off.  The versions they would have written are marked
+ * failed, and every request bound to one completes with CF_ERROR_CUDA. */
+CFCULL_API int cf_testing_fail_version_writes(int32_t n);
 
 #ifdef __cplusplus
 }

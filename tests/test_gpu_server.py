@@ -278,3 +278,55 @@ def test_pinned_registers_and_updates_are_copied_by_the_worker(gpu, oracle):
         srv.release(rid)
     srv.close()
     del pinned, flat
+
+
+def test_failed_version_writes_fail_their_requests_and_nothing_else(gpu, oracle, cflib):
+    """A queued jitter whose launch fails (a test hook fails it on the host,
+    nothing is launched): the batch that carried it reports CF_ERROR_CUDA,
+    later requests bound to the unwritten version (and to a jitter of it)
+    fail at admission, the idle-flush path fails the same way, and a new
+    version from the host brings the set back, bit-exact."""
+    import time
+
+    from hellovulkan_gb300.server import Server
+    from oracle import jitter_lights
+    CF_ERROR_CUDA = 3
+    srv = Server(gpu, budget_bytes=256 << 20, streams=1)
+    v = scenes.plain_small(9)
+    sid = srv.register(v.lights)  # pageable: copied before the call returns
+
+    def take(srv, count):
+        out = srv.wait_all(count, timeout_s=10.0)
+        assert len(out) == count, (srv.stats(), cflib.cf_last_error_message())
+        return {c.request_id: c for c in out}
+
+    try:
+        rid = srv.submit(v.ubo, sid)
+        assert take(srv, 1)[rid].status == 0
+        srv.release(rid)
+        cflib.cf_testing_fail_version_writes(1)
+        srv.jitter(sid, 5, 0.5)
+        carried = srv.submit(v.ubo, sid)  # its batch carries the failing launch
+        assert take(srv, 1)[carried].status == CF_ERROR_CUDA
+        later = srv.submit(v.ubo, sid)  # bound to the unwritten version
+        assert take(srv, 1)[later].status == CF_ERROR_CUDA
+        srv.jitter(sid, 6, 0.5)  # a jitter of it is unwritten too
+        rid = srv.submit(v.ubo, sid)
+        assert take(srv, 1)[rid].status == CF_ERROR_CUDA
+        srv.update(sid, v.lights)  # a new version from the host
+        cflib.cf_testing_fail_version_writes(1)
+        srv.jitter(sid, 7, 0.5)
+        time.sleep(0.05)  # no request: the idle flush fails
+        rid = srv.submit(v.ubo, sid)
+        assert take(srv, 1)[rid].status == CF_ERROR_CUDA
+        srv.update(sid, v.lights)
+        srv.jitter(sid, 8, 0.5)  # and works again
+        rid = srv.submit(v.ubo, sid)
+        c = take(srv, 1)[rid]
+        assert c.status == 0
+        cells, idx = srv.read(c)
+        oc, oi = oracle_result(oracle, v.ubo, jitter_lights(v.lights, 8, 0.5))
+        assert np.array_equal(cells, oc) and np.array_equal(idx, oi)
+    finally:
+        cflib.cf_testing_fail_version_writes(0)
+        srv.close()

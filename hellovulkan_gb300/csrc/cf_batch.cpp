@@ -4,8 +4,9 @@
 // buffers (caller-owned device memory).  One culling pass of the batch is
 //   batch_xform   every view's lights to view space            (1 launch)
 //   batch_bin     every view's depth-slice candidate lists      (1 launch)
-//   cull_batch    per shape bucket, a persistent kernel taking
-//                 (view, cluster group) items from a device queue (1 launch / bucket)
+//   cull_batch    a persistent kernel taking (view, cluster group) items
+//                 from a device queue (1 launch per run of shape buckets
+//                 with the same configuration, largest grids first)
 //   batch_scan    every view's group offsets                    (1 launch)
 //   batch_copy    every view's LightCells and index list        (1 launch)
 // and can be captured once into a CUDA graph and replayed while the views'
@@ -60,6 +61,15 @@ struct CfBatch {
         int ctas;
     };
     std::vector<Bucket> buckets;
+    // culling launches: consecutive buckets with the same configuration share
+    // one persistent launch over their (contiguous) items, so the batch pays
+    // one launch tail per configuration instead of one per grid
+    struct Launch {
+        cfk::CullConfig cfg;
+        uint32_t item_begin, item_count;
+        int ctas;
+    };
+    std::vector<Launch> launches;
     std::vector<cfk::ViewJob> jobs;
     uint32_t xform_blocks = 0, bin_blocks = 0, copy_blocks_total = 0, n_items = 0;
     size_t ws_bytes = 0;
@@ -124,6 +134,12 @@ cfk::CullConfig config_for(const CfBatch* b, uint32_t key)
 {
     auto it = b->tuned.find(key);
     return it == b->tuned.end() ? kBatchDefault : it->second;
+}
+
+bool same_config(const cfk::CullConfig& a, const cfk::CullConfig& c)
+{
+    return a.clusters_per_warp == c.clusters_per_warp && a.warps == c.warps && a.tile == c.tile &&
+           a.stages == c.stages && a.binned == c.binned;
 }
 
 int validate_view(const CfBatchView& v, uint32_t i, uint32_t* clusters)
@@ -229,20 +245,31 @@ int rebuild(CfBatch* b)
     if (by_key.size() > cfk::kMaxBatchQueues)
         return fail(CF_ERROR_INVALID_ARGUMENT, "%zu distinct grids exceed %u per batch", by_key.size(),
                     cfk::kMaxBatchQueues);
+    // largest grids first: their items are the longest, so within a launch
+    // shared with smaller grids they start in the first wave
     std::vector<uint2> items;
     b->buckets.clear();
-    for (auto& kv : by_key) {
-        std::vector<uint32_t>& vs = kv.second;
+    b->launches.clear();
+    for (auto it = by_key.rbegin(); it != by_key.rend(); ++it) {
+        std::vector<uint32_t>& vs = it->second;
         std::stable_sort(vs.begin(), vs.end(),
                          [&](uint32_t x, uint32_t y) { return b->jobs[x].light_count > b->jobs[y].light_count; });
-        CfBatch::Bucket bk{kv.first, config_for(b, kv.first), (uint32_t)items.size(), 0, 0};
+        CfBatch::Bucket bk{it->first, config_for(b, it->first), (uint32_t)items.size(), 0, 0};
         for (uint32_t vi : vs)
             for (uint32_t gi = 0; gi < b->jobs[vi].v.groups; ++gi) items.push_back(make_uint2(vi, gi));
         bk.item_count = (uint32_t)items.size() - bk.item_begin;
-        cudaError_t e = cfk::batch_cull_resident_ctas(bk.cfg, &bk.ctas);
+        int resident = 0;
+        cudaError_t e = cfk::batch_cull_resident_ctas(bk.cfg, &resident);
         if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
-        bk.ctas = std::min<int>(bk.ctas, (int)std::max<uint32_t>(bk.item_count, 1));
+        bk.ctas = std::min<int>(resident, (int)std::max<uint32_t>(bk.item_count, 1));
         b->buckets.push_back(bk);
+        if (!b->launches.empty() && same_config(b->launches.back().cfg, bk.cfg)) {
+            CfBatch::Launch& l = b->launches.back();
+            l.item_count += bk.item_count;
+            l.ctas = std::min<int>(resident, (int)std::max<uint32_t>(l.item_count, 1));
+        } else {
+            b->launches.push_back(CfBatch::Launch{bk.cfg, bk.item_begin, bk.item_count, bk.ctas});
+        }
     }
     b->n_items = (uint32_t)items.size();
     s = grow(reinterpret_cast<void**>(&b->d_jobs), &b->jobs_cap, std::max<size_t>(n, 1) * sizeof(cfk::ViewJob), "batch jobs");
@@ -268,12 +295,12 @@ int enqueue_batch(CfBatch* b, cudaStream_t st)
     const uint32_t* px = b->d_prefix;
     const uint32_t* pb = b->d_prefix + n;
     cudaError_t e = cfk::launch_batch_xform(b->d_jobs, px, n, b->xform_blocks, b->d_queues,
-                                            (uint32_t)b->buckets.size(), st);
+                                            (uint32_t)b->launches.size(), st);
     if (e == cudaSuccess) e = cfk::launch_batch_bin(b->d_jobs, pb, b->d_prefix + 3 * (size_t)n, n, b->bin_blocks, st);
-    for (size_t q = 0; q < b->buckets.size() && e == cudaSuccess; ++q) {
-        const CfBatch::Bucket& bk = b->buckets[q];
-        cfk::BatchCull bc{b->d_jobs, b->d_items + bk.item_begin, bk.item_count, b->d_queues + q};
-        e = cfk::launch_batch_cull(bc, bk.cfg, bk.ctas, b->dev_error, st);
+    for (size_t q = 0; q < b->launches.size() && e == cudaSuccess; ++q) {
+        const CfBatch::Launch& l = b->launches[q];
+        cfk::BatchCull bc{b->d_jobs, b->d_items + l.item_begin, l.item_count, b->d_queues + q};
+        e = cfk::launch_batch_cull(bc, l.cfg, l.ctas, b->dev_error, st);
     }
     if (e == cudaSuccess) e = cfk::launch_batch_scan(b->d_jobs, n, st);
     if (e == cudaSuccess) e = cfk::launch_batch_copy(b->d_jobs, b->d_prefix + 2 * (size_t)n, n, b->copy_blocks_total, st);

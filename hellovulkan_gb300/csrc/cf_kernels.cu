@@ -33,6 +33,7 @@
 #include "cf_device.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <utility>
 
 #include "cf_pinned_math.h"
@@ -1896,9 +1897,31 @@ cudaError_t launch_batch_cull(const BatchCull& b, const CullConfig& cfg, int cta
 
 cudaError_t batch_cull_resident_ctas(const CullConfig& cfg, int* ctas)
 {
-    int dev = 0, sms = 0, per_sm = 0;
+    // per device and configuration, queried once: a server asks for every
+    // batch it launches, and each query is several CUDA calls
+    constexpr int kDevices = 16, kConfigs = 32;
+    static std::atomic<int> cache[kDevices][kConfigs];  // 0: not yet known
+    int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    int slot = -1, index = 0;
+#define CF_SLOT(K, W, T, S, B)                                                                                  \
+    if (cfg.clusters_per_warp == K && cfg.warps == W && cfg.tile == T && cfg.stages == S && (cfg.binned != 0) == B) \
+        slot = index;                                                                                             \
+    ++index;
+    CF_CULL_CONFIGS(CF_SLOT)
+#undef CF_SLOT
+    static_assert(kConfigs >= 18, "one cache slot per configuration");
+    const bool cached = dev >= 0 && dev < kDevices && slot >= 0;
+    if (cached) {
+        const int c = cache[dev][slot].load(std::memory_order_relaxed);
+        if (c > 0) {
+            *ctas = c;
+            return cudaSuccess;
+        }
+    }
+    int sms = 0, per_sm = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
 #define CF_OCC(K, W, T, S, B)                                                                                   \
     if (cfg.clusters_per_warp == K && cfg.warps == W && cfg.tile == T && cfg.stages == S && (cfg.binned != 0) == B) \
@@ -1907,6 +1930,7 @@ cudaError_t batch_cull_resident_ctas(const CullConfig& cfg, int* ctas)
 #undef CF_OCC
     if (e != cudaSuccess) return e;
     *ctas = sms * (per_sm > 0 ? per_sm : 1);
+    if (cached) cache[dev][slot].store(*ctas, std::memory_order_relaxed);
     return cudaSuccess;
 }
 

@@ -504,13 +504,20 @@ void fill_tables(CfServer* s, int slot_i, const std::vector<Request*>& reqs, Lau
         cb += cfk::copy_blocks(r->groups);
         buckets[j.v.slice_clusters].push_back(i);
     }
+    // largest grids first; consecutive grids with the same configuration share
+    // one culling launch over their contiguous items (one launch tail fewer)
     uint32_t ni = 0;
-    for (auto& kv : buckets) {
-        LaunchPlan::Bucket bk{reqs[kv.second[0]]->cfg, ni, 0};
-        for (uint32_t vi : kv.second)
+    for (auto kv = buckets.rbegin(); kv != buckets.rend(); ++kv) {
+        const cfk::CullConfig& cfg = reqs[kv->second[0]]->cfg;
+        const uint32_t begin = ni;
+        for (uint32_t vi : kv->second)
             for (uint32_t g = 0; g < jobs[vi].v.groups; ++g) it[ni++] = make_uint2(vi, g);
-        bk.count = ni - bk.begin;
-        plan.buckets.push_back(bk);
+        LaunchPlan::Bucket* last = plan.buckets.empty() ? nullptr : &plan.buckets.back();
+        if (last && last->cfg.clusters_per_warp == cfg.clusters_per_warp && last->cfg.warps == cfg.warps &&
+            last->cfg.tile == cfg.tile && last->cfg.stages == cfg.stages && last->cfg.binned == cfg.binned)
+            last->count = ni - last->begin;
+        else
+            plan.buckets.push_back(LaunchPlan::Bucket{cfg, begin, ni - begin});
     }
     plan.xform_blocks = xb;
     plan.bin_blocks = bb;

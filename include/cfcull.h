@@ -280,7 +280,7 @@ typedef struct CfServerConfig {
     uint64_t hbm_budget_bytes;     /* device memory for light sets, AABBs, scratch and outputs (default 8 GiB) */
     uint32_t max_batch_views;      /* views per launch (default 64)                                         */
     uint32_t streams;              /* batches in flight at once (default 4)                                  */
-    uint32_t max_pending;          /* submissions waiting for admission (default 2^20)                      */
+    uint32_t max_pending;          /* submissions waiting for admission (default 4096; past it CF_ERROR_BUDGET) */
     uint32_t max_groups_per_view;  /* largest view, in cluster groups (default 16384)                        */
 } CfServerConfig;
 

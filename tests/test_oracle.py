@@ -342,3 +342,36 @@ def test_oracle_consumers_match_golden(oracle, golden_consumers):
     out = oracle.shade_clusters(ubo_from_bytes(g["negzero/ubo"]), np.zeros(3), CfPBRPushConstant(
         *g["negzero/pc"].tolist()), g["negzero/gbuffer"], g["negzero/cells"], g["negzero/indices"], g["negzero/lights"])
     assert np.array_equal(bits(out[..., :3]), g["negzero/shade_rgb"])
+
+
+def test_jitter_restatement_follows_the_documented_formula():
+    """oracle.jitter_lights (the host restatement the server's GPU tests check
+    against) against the formula documented at cf_server_jitter_light_set in
+    include/cfcull.h, restated here independently with Python integers and
+    float32 scalars, one rounding per operation."""
+    import numpy as np
+
+    from hellovulkan_gb300 import scenes
+    from oracle import jitter_lights
+    M = (1 << 64) - 1
+
+    def mix(x):
+        x ^= x >> 30
+        x = (x * 0xBF58476D1CE4E5B9) & M
+        x ^= x >> 27
+        x = (x * 0x94D049BB133111EB) & M
+        return x ^ (x >> 31)
+
+    rng = np.random.default_rng(41)
+    lights = scenes.uniform_box_lights(rng, 9, [-20, -10, -60], [20, 10, -1], 1.0, 6.0)
+    for seed, sigma in ((0, 0.1), (123456789, 0.75), ((1 << 64) - 3, 2.5)):
+        got = jitter_lights(lights, seed, sigma)
+        for i in range(lights.shape[0]):
+            for a in range(3):
+                s = np.float32(0.0)
+                for k in range(12):
+                    h = mix((seed + i * 0x9E3779B97F4A7C15 + (a * 12 + k) * 0xD1B54A32D192ED03) & M)
+                    s = np.float32(s + np.float32(np.float32(h >> 40) * np.float32(2.0 ** -24)))
+                want = np.float32(lights[i, a] + np.float32(np.float32(sigma) * np.float32(s - np.float32(6.0))))
+                assert got[i, a].view(np.uint32) == want.view(np.uint32), (seed, i, a)
+        assert np.array_equal(got[:, 3:].view(np.uint32), lights[:, 3:].view(np.uint32))  # only x, y, z move

@@ -375,3 +375,30 @@ def test_jitter_restatement_follows_the_documented_formula():
                 want = np.float32(lights[i, a] + np.float32(np.float32(sigma) * np.float32(s - np.float32(6.0))))
                 assert got[i, a].view(np.uint32) == want.view(np.uint32), (seed, i, a)
         assert np.array_equal(got[:, 3:].view(np.uint32), lights[:, 3:].view(np.uint32))  # only x, y, z move
+
+
+def test_orbit_restatement_follows_the_documented_rotation():
+    """oracle.animate_orbits (what the animated workload's GPU checks compare
+    against) against CfLightOrbit's documented step, offset' = R * offset with
+    R = [[cos, -sin], [sin, cos]], then position = (cx + x, cy, cz + z, cw):
+    restated per light with float32 scalars, products before the difference
+    or sum, one rounding per operation."""
+    import numpy as np
+    from oracle import animate_orbits
+    rng = np.random.default_rng(43)
+    n = 7
+    o = np.zeros((n, 8), np.float32)
+    o[:, 0:2] = rng.uniform(-10, 10, (n, 2))
+    ang = rng.uniform(0.001, 0.05, n)
+    o[:, 2], o[:, 3] = np.cos(ang), np.sin(ang)
+    o[:, 4:7] = rng.uniform(-50, 50, (n, 3))
+    o[:, 7] = 1.0
+    got_o, got_p = animate_orbits(o, 13)
+    for i in range(n):
+        x, z, c, s = o[i, 0], o[i, 1], o[i, 2], o[i, 3]
+        for _ in range(13):
+            x, z = (np.float32(np.float32(c * x) - np.float32(s * z)), np.float32(np.float32(s * x) + np.float32(c * z)))
+        want_p = np.array([np.float32(o[i, 4] + x), o[i, 5], np.float32(o[i, 6] + z), o[i, 7]], np.float32)
+        assert got_o[i, 0].view(np.uint32) == np.float32(x).view(np.uint32)
+        assert got_o[i, 1].view(np.uint32) == np.float32(z).view(np.uint32)
+        assert np.array_equal(got_p[i].view(np.uint32), want_p.view(np.uint32)), i
